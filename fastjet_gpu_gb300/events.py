@@ -1,0 +1,191 @@
+"""Seeded synthetic event generators and the reference's text event format.
+
+Events are massless (E = |p|) particles in FP64, built from hard jet axes plus
+a soft background, following the workload definitions this library is measured
+on:
+
+* ``single_event``  -- one event of N particles with ``n_axes`` hard axes
+  (eta U[-2.5, 2.5], phi U[-pi, pi), axis pT from a 1/pT^4 spectrum above
+  30 GeV, Poisson(15) constituents per axis with Dirichlet(1) momentum
+  fractions and Gaussian sigma=0.1 angular offsets) and a soft background
+  (pT Exp(mean 0.7 GeV) floored at 0.1 GeV, eta U[-5, 5]).
+* ``mixed_batch``   -- particle counts log-uniform in [lo, hi], Poisson(3)+1 axes.
+* ``pileup_batch``  -- 10k-60k particles: soft pT Exp(0.6 GeV), eta U[-4, 4],
+  plus 2-6 hard axes.
+* ``serving_sizes`` -- lognormal sizes (median 1500, sigma 0.8) clipped to
+  [100, 20000] and the algorithm mix 70% anti-kt R=0.4, 15% kt R=0.6,
+  15% C/A R=0.8.
+
+The text format is the reference driver's input stream (main.cc:34-70): four
+numbers ``px py pz E`` per line, an event ends at the first blank line or line
+starting with '#'.
+
+A batch is held as CSR: ``particles`` float64 [total, 4] (px, py, pz, E) and
+``offsets`` int64 [n_events + 1].
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+TWO_PI = 2.0 * math.pi
+
+
+def _massless(pt, eta, phi):
+    px = pt * np.cos(phi)
+    py = pt * np.sin(phi)
+    pz = pt * np.sinh(eta)
+    E = pt * np.cosh(eta)
+    return np.stack([px, py, pz, E], axis=1)
+
+
+def _hard_axes(rng, n_axes, n_max, eta_span=2.5):
+    """Constituents of ``n_axes`` hard axes, at most ``n_max`` particles."""
+    pts, etas, phis = [], [], []
+    for _ in range(n_axes):
+        axis_pt = 30.0 * rng.random() ** (-1.0 / 3.0)  # dN/dpT ~ pT^-4 above 30 GeV
+        axis_eta = rng.uniform(-eta_span, eta_span)
+        axis_phi = rng.uniform(-math.pi, math.pi)
+        k = int(rng.poisson(15))
+        if k == 0:
+            continue
+        frac = rng.dirichlet(np.ones(k)) if k > 1 else np.ones(1)
+        pts.append(axis_pt * frac)
+        etas.append(axis_eta + rng.normal(0.0, 0.1, k))
+        phis.append(axis_phi + rng.normal(0.0, 0.1, k))
+    if not pts:
+        return np.zeros(0), np.zeros(0), np.zeros(0)
+    pt = np.concatenate(pts)[:n_max]
+    eta = np.concatenate(etas)[:n_max]
+    phi = np.concatenate(phis)[:n_max]
+    return pt, eta, phi
+
+
+def single_event(n, n_axes, seed, soft_mean=0.7, soft_eta=5.0):
+    """One event of exactly ``n`` massless particles, float64 [n, 4]."""
+    rng = np.random.default_rng(seed)
+    pt_h, eta_h, phi_h = _hard_axes(rng, n_axes, n)
+    n_soft = n - pt_h.size
+    pt_s = np.maximum(rng.exponential(soft_mean, n_soft), 0.1)
+    eta_s = rng.uniform(-soft_eta, soft_eta, n_soft)
+    phi_s = rng.uniform(-math.pi, math.pi, n_soft)
+    pt = np.concatenate([pt_h, pt_s])
+    eta = np.concatenate([eta_h, eta_s])
+    phi = np.concatenate([phi_h, phi_s])
+    order = rng.permutation(n)
+    return np.ascontiguousarray(_massless(pt[order], eta[order], phi[order]))
+
+
+@dataclass
+class Batch:
+    particles: np.ndarray  # float64 [total, 4]
+    offsets: np.ndarray  # int64 [n_events + 1]
+
+    @property
+    def n_events(self):
+        return self.offsets.size - 1
+
+    def sizes(self):
+        return np.diff(self.offsets)
+
+    def event(self, e):
+        return self.particles[self.offsets[e]:self.offsets[e + 1]]
+
+
+def _batch_from(events):
+    sizes = np.array([ev.shape[0] for ev in events], dtype=np.int64)
+    offsets = np.zeros(len(events) + 1, dtype=np.int64)
+    np.cumsum(sizes, out=offsets[1:])
+    parts = np.concatenate(events, axis=0) if events else np.zeros((0, 4))
+    return Batch(np.ascontiguousarray(parts, dtype=np.float64), offsets)
+
+
+def mixed_batch(n_events=4096, lo=50, hi=2000, seed=3):
+    """Events with particle counts log-uniform in [lo, hi], Poisson(3)+1 axes."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), n_events)).astype(np.int64)
+    sizes = np.clip(sizes, lo, hi)
+    axes = rng.poisson(3, n_events) + 1
+    seeds = rng.integers(0, 2**62, n_events)
+    return _batch_from([single_event(int(n), int(a), int(s)) for n, a, s in zip(sizes, axes, seeds)])
+
+
+def pileup_batch(n_events=64, lo=10000, hi=60000, seed=4):
+    """Pile-up-like events: soft pT Exp(0.6), eta U[-4, 4], 2-6 hard axes."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(lo, hi + 1, n_events)
+    axes = rng.integers(2, 7, n_events)
+    seeds = rng.integers(0, 2**62, n_events)
+    return _batch_from([single_event(int(n), int(a), int(s), soft_mean=0.6, soft_eta=4.0)
+                        for n, a, s in zip(sizes, axes, seeds)])
+
+
+ALGO_KT, ALGO_CAM, ALGO_ANTIKT = 1, 0, -1
+
+
+def serving_mix(n_events, seed=5, median=1500.0, sigma=0.8, lo=100, hi=20000):
+    """Sizes and (algorithm, R) per request for the served workload."""
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.exp(rng.normal(math.log(median), sigma, n_events)), lo, hi).astype(np.int64)
+    u = rng.random(n_events)
+    algo = np.where(u < 0.70, ALGO_ANTIKT, np.where(u < 0.85, ALGO_KT, ALGO_CAM)).astype(np.int32)
+    radius = np.where(u < 0.70, 0.4, np.where(u < 0.85, 0.6, 0.8))
+    axes = rng.poisson(3, n_events) + 1
+    seeds = rng.integers(0, 2**62, n_events)
+    batch = _batch_from([single_event(int(n), int(a), int(s)) for n, a, s in zip(sizes, axes, seeds)])
+    return batch, algo, radius
+
+
+# ---------------------------------------------------------------- text format
+
+def read_events(path_or_text):
+    """Parse the reference driver's event stream into a list of [n, 4] arrays.
+
+    Follows main.cc:34-70: leading '#' and blank lines are skipped, each line
+    holds px py pz E, an event ends at the first line that does not parse as
+    four numbers; such a line must be blank or start with '#', otherwise a
+    ValueError is raised (main.cc:55-58 throws).
+    """
+    if "\n" in path_or_text or not path_or_text:
+        text = path_or_text
+    else:
+        with open(path_or_text) as f:
+            text = f.read()
+    events, cur = [], []
+    for line in text.split("\n"):
+        fields = line.split()
+        vals = None
+        if len(fields) >= 4:
+            try:
+                vals = [float(x) for x in fields[:4]]
+            except ValueError:
+                vals = None
+        if vals is not None:
+            cur.append(vals)
+            continue
+        if line and line[0] != "#" and cur:
+            raise ValueError("Error while parsing particles:\n" + line)
+        if line and line[0] != "#" and not cur and line.strip():
+            raise ValueError("Error while parsing particles:\n" + line)
+        if cur:
+            events.append(np.array(cur, dtype=np.float64))
+            cur = []
+    if cur:
+        events.append(np.array(cur, dtype=np.float64))
+    return events
+
+
+def write_events(events, path=None):
+    """Write events in the reference's text format ('%.17g', exact round trip)."""
+    out = []
+    for ev in events:
+        for px, py, pz, E in ev:
+            out.append(f"{px:.17g} {py:.17g} {pz:.17g} {E:.17g}")
+        out.append("")
+    text = "\n".join(out)
+    if path is not None:
+        with open(path, "w") as f:
+            f.write(text)
+    return text

@@ -1,0 +1,127 @@
+/* fastjet_gb300: GB300-native sequential-recombination jet clustering.
+ *
+ * C ABI of libfastjet_gb300.so.  All entry points return an fjg_status and
+ * never abort.  Buffers are owned by the caller; device pointers must be
+ * device-accessible on the context's device.  Calls that take a stream are
+ * stream-ordered (asynchronous with respect to the host) unless stated.
+ *
+ * Reference interface replaced (fwyzard/fastjet_gpu):
+ *   cluster.h:4   enum class Algorithm { Kt = 1, CambridgeAachen = 0, AntiKt = -1 }
+ *                 -> FJG_KT / FJG_CAM / FJG_ANTIKT (same values, the exponent p)
+ *   PseudoJet.h:4 struct PseudoJet { int index; bool isJet; double px, py, pz, E; }
+ *                 -> fjg_pseudojet (identical layout, 40 bytes)
+ *   cluster.h:6   void cluster(PseudoJet *particles, int size, Algorithm algo, double r)
+ *                 -> fjg_cluster_pseudojets (same in-place device-buffer contract),
+ *                    and the unchanged C++ symbol in fastjet_gb300_compat.h
+ *   main.cc:269-335 per-event loop of the driver (H2D copy, cluster, D2H copy,
+ *                 isJet/ptmin filter, pT sort)
+ *                 -> fjg_cluster_batch / fjg_cluster_batch_host for many events
+ *                    per call, fjg_serve_* for events arriving over time.
+ */
+#ifndef FASTJET_GB300_H
+#define FASTJET_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FJG_OK = 0,
+  FJG_EINVAL = 1,     /* invalid argument (null pointer, bad algorithm, negative size, R <= 0) */
+  FJG_ENOMEM = 2,     /* device or host allocation failed */
+  FJG_ECUDA = 3,      /* a CUDA runtime call failed; fjg_last_error() has the message */
+  FJG_ETOOBIG = 4,    /* an event exceeds the supported particle count */
+  FJG_ETIMEDOUT = 5,  /* a bounded device wait ran out (serving queue) */
+  FJG_EAGAIN = 6,     /* serving: no free slot or result not ready yet */
+  FJG_EKERNEL = 7     /* a kernel reported an internal inconsistency */
+} fjg_status;
+
+/* Algorithm codes: the reference enum values (cluster.h:4). */
+#define FJG_KT 1
+#define FJG_CAM 0
+#define FJG_ANTIKT (-1)
+
+/* Largest event the library clusters (particles per event). */
+#define FJG_MAX_EVENT_PARTICLES 262144
+
+/* I/O record of the reference (PseudoJet.h:4-11): 40 bytes, px at offset 8. */
+typedef struct {
+  int index;
+  _Bool isJet;
+  double px, py, pz, E;
+} fjg_pseudojet;
+
+/* One clustering step: a merge of pseudojets a < b, or (b == -1) the promotion
+ * of a to a final jet; d is the winning distance.  A pseudojet's label is the
+ * lowest input index among its constituents. */
+typedef struct {
+  int32_t a;
+  int32_t b;
+  double d;
+} fjg_step;
+
+/* Outputs of a batch, CSR-indexed by the batch's offsets (event e owns
+ * [offsets[e], offsets[e+1])).  Jets of event e are jets[offsets[e] + k],
+ * k < n_jets[e], in promotion order.  history and owner may be NULL. */
+typedef struct {
+  double* jets;       /* [total][4] px, py, pz, E */
+  int32_t* jet_label; /* [total] label of each jet */
+  int32_t* n_jets;    /* [n_events] */
+  fjg_step* history;  /* [total] optional: one record per step */
+  int32_t* owner;     /* [total] optional: for each input particle, index k of its jet */
+} fjg_outputs;
+
+typedef struct fjg_ctx fjg_ctx;
+
+/* Create a context on `device` (a CUDA ordinal).  The context owns a stream,
+ * cached scratch memory and captured CUDA graphs.  Thread-safe per context
+ * only under external serialisation. */
+fjg_status fjg_ctx_create(int device, fjg_ctx** out);
+void fjg_ctx_destroy(fjg_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t). */
+void* fjg_ctx_stream(fjg_ctx* ctx);
+const char* fjg_status_string(fjg_status s);
+/* Last error message of the context (or of the calling thread when ctx is NULL). */
+const char* fjg_last_error(const fjg_ctx* ctx);
+
+/* Batched clustering of device-resident events (the persistent-kernel path).
+ *   p4      device [total][4] FP64 px, py, pz, E
+ *   offsets device [n_events + 1] int64, offsets[0] == 0
+ *   algo    device [n_events] int32 or NULL (then algo_all for every event)
+ *   radius  device [n_events] FP64 or NULL (then r_all for every event)
+ *   total   offsets[n_events] (host value; sizes the scratch)
+ *   stream  cudaStream_t or NULL for the context stream
+ * Events are clustered independently; results do not depend on batch
+ * composition. */
+fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offsets, int n_events, int64_t total,
+                             const int32_t* algo, int algo_all, const double* radius, double r_all,
+                             const fjg_outputs* out, void* stream);
+
+/* Same, with every buffer in host memory (pinned or pageable).  Copies the
+ * inputs to the device, clusters, copies the outputs back, and synchronises. */
+fjg_status fjg_cluster_batch_host(fjg_ctx* ctx, const double* p4, const int64_t* offsets, int n_events,
+                                  const int32_t* algo, int algo_all, const double* radius, double r_all,
+                                  const fjg_outputs* out);
+
+/* The plain path: one event per launch on the context stream, one CTA,
+ * synchronous.  Device buffers as in fjg_cluster_batch for a single event. */
+fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, double r, double* jets,
+                             int32_t* jet_label, int32_t* n_jets, fjg_step* history, int32_t* owner);
+
+/* Drop-in for the reference's cluster() (cluster.h:6): `particles` is a device
+ * buffer of `size` records, rewritten in place.  On return every record has
+ * index = its input position; records whose slot holds a final jet have
+ * isJet = true and the jet's momentum (the jet sits at the slot of its
+ * lowest-index constituent); all other records have isJet = false.
+ * Synchronous on the given stream (NULL: the context stream). */
+fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int size, int algo, double r,
+                                  void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTJET_GB300_H */
