@@ -1,0 +1,249 @@
+"""GB300-native sequential-recombination jet clustering (kt, Cambridge/Aachen, anti-kt).
+
+Python host mirror of the library's C ABI (include/fastjet_gb300.h), loaded
+from the in-tree build fastjet_gpu_gb300/_lib/libfastjet_gb300.so.  There is no
+CPU fallback: every call runs the CUDA kernels, and importing the bindings
+raises if the library has not been built.
+
+Reference interface mirrored (fwyzard/fastjet_gpu):
+  * ``Algorithm``            -- cluster.h:4 ``enum class Algorithm {Kt=1, CambridgeAachen=0, AntiKt=-1}``
+  * ``PSEUDOJET``            -- PseudoJet.h:4-11, the 40-byte I/O record
+  * ``cluster(records, size, algo, r)`` -- cluster.h:6, in-place clustering of
+    PseudoJet records (numpy structured array on the host, or a CUDA tensor of
+    raw records on the device)
+  * ``Context.cluster_batch`` / ``cluster_batch_device`` -- many events per call
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libfastjet_gb300.so")
+
+
+class Algorithm(enum.IntEnum):
+    Kt = 1
+    CambridgeAachen = 0
+    AntiKt = -1
+
+
+KT, CAM, ANTIKT = 1, 0, -1
+
+PSEUDOJET = np.dtype({"names": ["index", "isJet", "px", "py", "pz", "E"],
+                      "formats": ["<i4", "?", "<f8", "<f8", "<f8", "<f8"],
+                      "offsets": [0, 4, 8, 16, 24, 32], "itemsize": 40})
+STEP = np.dtype([("a", "<i4"), ("b", "<i4"), ("d", "<f8")])
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "event too large",
+          5: "timed out", 6: "try again", 7: "kernel error"}
+
+
+class FjgError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class _Outputs(ctypes.Structure):
+    _fields_ = [("jets", ctypes.c_void_p), ("jet_label", ctypes.c_void_p), ("n_jets", ctypes.c_void_p),
+                ("history", ctypes.c_void_p), ("owner", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded C library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m fastjet_gpu_gb300.build` first")
+        L = ctypes.CDLL(LIB_PATH)
+        P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        L.fjg_ctx_create.argtypes = [I, ctypes.POINTER(P)]
+        L.fjg_ctx_destroy.argtypes = [P]
+        L.fjg_ctx_destroy.restype = None
+        L.fjg_ctx_stream.argtypes = [P]
+        L.fjg_ctx_stream.restype = P
+        L.fjg_ctx_check.argtypes = [P]
+        L.fjg_last_error.argtypes = [P]
+        L.fjg_last_error.restype = ctypes.c_char_p
+        L.fjg_status_string.argtypes = [I]
+        L.fjg_status_string.restype = ctypes.c_char_p
+        L.fjg_cluster_batch.argtypes = [P, P, P, I, ctypes.c_int64, P, I, P, D, ctypes.POINTER(_Outputs), P]
+        L.fjg_cluster_batch_host.argtypes = [P, P, P, I, P, I, P, D, ctypes.POINTER(_Outputs)]
+        L.fjg_cluster_event.argtypes = [P, P, I, I, D, P, P, P, P, P]
+        L.fjg_cluster_pseudojets.argtypes = [P, P, I, I, D, P]
+        _lib = L
+    return _lib
+
+
+def _np_ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _t_ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class Context:
+    """A library context on one CUDA device (stream, scratch, side streams)."""
+
+    def __init__(self, device=0):
+        self._h = ctypes.c_void_p()
+        st = lib().fjg_ctx_create(int(device), ctypes.byref(self._h))
+        if st:
+            raise FjgError(st, lib().fjg_last_error(None).decode())
+        self.device = device
+
+    def close(self):
+        if self._h:
+            lib().fjg_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st:
+            raise FjgError(st, lib().fjg_last_error(self._h).decode())
+
+    @property
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        return lib().fjg_ctx_stream(self._h)
+
+    def check(self):
+        self._check(lib().fjg_ctx_check(self._h))
+
+    # ------------------------------------------------------------ host memory
+    def cluster_batch(self, particles, offsets, algo, radius, history=False, owner=False):
+        """Cluster a CSR batch held in host memory; returns numpy arrays.
+
+        particles float64 [total, 4]; offsets int64 [n_events + 1]; algo and
+        radius are scalars or per-event arrays.  Returns a dict with ``jets``
+        [total, 4], ``jet_label`` [total], ``n_jets`` [n_events] and, when
+        requested, ``history`` (STEP records) and ``owner``.
+        """
+        p4 = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 4)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        ne = off.size - 1
+        total = int(off[-1]) if ne >= 0 else 0
+        a_arr = None if np.isscalar(algo) else np.ascontiguousarray(algo, dtype=np.int32)
+        r_arr = None if np.isscalar(radius) else np.ascontiguousarray(radius, dtype=np.float64)
+        res = {"jets": np.zeros((max(total, 1), 4)), "jet_label": np.zeros(max(total, 1), np.int32),
+               "n_jets": np.zeros(max(ne, 1), np.int32)}
+        if history:
+            res["history"] = np.zeros(max(total, 1), STEP)
+        if owner:
+            res["owner"] = np.zeros(max(total, 1), np.int32)
+        out = _Outputs(_np_ptr(res["jets"]).value, _np_ptr(res["jet_label"]).value, _np_ptr(res["n_jets"]).value,
+                       _np_ptr(res["history"]).value if history else None,
+                       _np_ptr(res["owner"]).value if owner else None)
+        st = lib().fjg_cluster_batch_host(self._h, _np_ptr(p4), _np_ptr(off), ne, _np_ptr(a_arr),
+                                          int(algo) if a_arr is None else 0, _np_ptr(r_arr),
+                                          float(radius) if r_arr is None else 0.0, ctypes.byref(out))
+        self._check(st)
+        res["jets"] = res["jets"][:total]
+        res["jet_label"] = res["jet_label"][:total]
+        res["n_jets"] = res["n_jets"][:ne]
+        if history:
+            res["history"] = res["history"][:total]
+        if owner:
+            res["owner"] = res["owner"][:total]
+        return res
+
+    # ---------------------------------------------------------- device memory
+    def cluster_batch_device(self, p4, offsets, algo, radius, total=None, history=False, owner=False, out=None,
+                             stream=None):
+        """Cluster device-resident torch CUDA tensors (asynchronous on the stream).
+
+        p4 float64 [total, 4]; offsets int64 [n_events + 1]; algo/radius scalars
+        or int32/float64 tensors.  ``out`` may pass preallocated outputs.
+        """
+        import torch
+        ne = offsets.numel() - 1
+        total = p4.shape[0] if total is None else total
+        if out is None:
+            dev = p4.device
+            out = {"jets": torch.empty((max(total, 1), 4), dtype=torch.float64, device=dev),
+                   "jet_label": torch.empty(max(total, 1), dtype=torch.int32, device=dev),
+                   "n_jets": torch.empty(max(ne, 1), dtype=torch.int32, device=dev)}
+            if history:
+                out["history"] = torch.empty((max(total, 1), 2), dtype=torch.float64, device=dev)
+            if owner:
+                out["owner"] = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+        o = _Outputs(out["jets"].data_ptr(), out["jet_label"].data_ptr(), out["n_jets"].data_ptr(),
+                     out["history"].data_ptr() if "history" in out else None,
+                     out["owner"].data_ptr() if "owner" in out else None)
+        a_t = None if isinstance(algo, (int, np.integer)) else algo
+        r_t = None if isinstance(radius, (float, int, np.floating)) else radius
+        st = lib().fjg_cluster_batch(self._h, _t_ptr(p4), _t_ptr(offsets), ne, int(total), _t_ptr(a_t),
+                                     int(algo) if a_t is None else 0, _t_ptr(r_t),
+                                     float(radius) if r_t is None else 0.0, ctypes.byref(o),
+                                     ctypes.c_void_p(stream) if stream else None)
+        self._check(st)
+        return out
+
+    def cluster_event(self, p4, algo, radius, history=False, owner=False):
+        """The plain path: one event per launch (torch CUDA tensors), synchronous."""
+        import torch
+        n = p4.shape[0]
+        dev = p4.device
+        out = {"jets": torch.empty((max(n, 1), 4), dtype=torch.float64, device=dev),
+               "jet_label": torch.empty(max(n, 1), dtype=torch.int32, device=dev),
+               "n_jets": torch.empty(1, dtype=torch.int32, device=dev)}
+        if history:
+            out["history"] = torch.empty((max(n, 1), 2), dtype=torch.float64, device=dev)
+        if owner:
+            out["owner"] = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        st = lib().fjg_cluster_event(self._h, _t_ptr(p4), n, int(algo), float(radius), _t_ptr(out["jets"]),
+                                     _t_ptr(out["jet_label"]), _t_ptr(out["n_jets"]),
+                                     _t_ptr(out.get("history")), _t_ptr(out.get("owner")))
+        self._check(st)
+        return out
+
+    def cluster_pseudojets(self, records, size, algo, radius):
+        """In-place clustering of PseudoJet records (cluster.h:6 semantics).
+
+        ``records``: a numpy PSEUDOJET array (host; copied to the device and
+        back) or a CUDA torch uint8 tensor of ``size * 40`` bytes (in place).
+        """
+        import torch
+        if isinstance(records, np.ndarray):
+            assert records.dtype == PSEUDOJET
+            host = records
+            dev = torch.from_numpy(records.view(np.uint8).reshape(-1).copy()).cuda(self.device)
+        else:
+            host, dev = None, records
+        st = lib().fjg_cluster_pseudojets(self._h, _t_ptr(dev), int(size), int(algo), float(radius), None)
+        self._check(st)
+        if host is not None:
+            host.view(np.uint8).reshape(-1)[:] = dev.cpu().numpy()
+        return records
+
+
+_default_ctx = {}
+
+
+def default_context(device=0):
+    if device not in _default_ctx:
+        _default_ctx[device] = Context(device)
+    return _default_ctx[device]
+
+
+def cluster(records, size, algo, r):
+    """Drop-in for the reference's ``cluster(PseudoJet*, int, Algorithm, double)``."""
+    return default_context().cluster_pseudojets(records, size, int(algo), r)
+
+
+def history_records(t):
+    """View a device history tensor (float64 [n, 2]) as numpy STEP records."""
+    return t.cpu().numpy().view(STEP).reshape(-1)

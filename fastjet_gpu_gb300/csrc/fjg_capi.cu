@@ -1,0 +1,360 @@
+// C ABI of libfastjet_gb300.so (declarations: include/fastjet_gb300.h).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "fastjet_gb300.h"
+#include "fjg_kernels.cuh"
+
+using fjg::BatchArgs;
+
+namespace {
+
+thread_local std::string g_thread_error;
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) {
+      cudaDeviceSynchronize();  // the old buffer may still be in use by queued work
+      cudaFree(ptr);
+    }
+    ptr = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 4 + 256;
+    cudaError_t err = cudaMalloc(&ptr, want);
+    if (err == cudaSuccess) cap = want;
+    return err;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace
+
+struct fjg_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t side[fjg::kNumBuckets] = {};
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t ev_join[fjg::kNumBuckets] = {};
+  fjg::Scratch sc{};
+  DeviceBuffer scratch;  // order/counts/queues/status/offsets1
+  DeviceBuffer io;       // device copies for the host-memory entry points
+  DeviceBuffer single;   // outputs of fjg_cluster_pseudojets
+  std::string last_error;
+};
+
+namespace {
+
+fjg_status set_error(fjg_ctx* ctx, fjg_status st, const std::string& msg) {
+  if (ctx)
+    ctx->last_error = msg;
+  else
+    g_thread_error = msg;
+  return st;
+}
+
+fjg_status cuda_error(fjg_ctx* ctx, cudaError_t err, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(err) + ": " + cudaGetErrorString(err);
+  return set_error(ctx, err == cudaErrorMemoryAllocation ? FJG_ENOMEM : FJG_ECUDA, m);
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Ensure the device scratch can describe `n_events` events.
+cudaError_t ensure_scratch(fjg_ctx* ctx, int n_events) {
+  if (n_events < 1) n_events = 1;
+  if (ctx->sc.order && ctx->sc.cap_events >= n_events) return cudaSuccess;
+  int cap = n_events + n_events / 4 + 64;
+  size_t bytes = sizeof(int32_t) * (size_t)fjg::kNumBuckets * cap + 64 * 4 + 64;
+  cudaError_t err = ctx->scratch.reserve(bytes);
+  if (err != cudaSuccess) return err;
+  char* p = static_cast<char*>(ctx->scratch.ptr);
+  ctx->sc.offsets1 = reinterpret_cast<int64_t*>(p);
+  ctx->sc.counts = reinterpret_cast<int32_t*>(p + 64);
+  ctx->sc.queues = reinterpret_cast<int*>(p + 128);
+  ctx->sc.status = reinterpret_cast<int*>(p + 192);
+  ctx->sc.order = reinterpret_cast<int32_t*>(p + 256);
+  ctx->sc.cap_events = cap;
+  err = cudaMemset(ctx->sc.status, 0, sizeof(int));
+  if (err == cudaSuccess) err = cudaDeviceSynchronize();
+  return err;
+}
+
+bool valid_algo(int a) { return a == FJG_KT || a == FJG_CAM || a == FJG_ANTIKT; }
+
+// Read and clear the kernels' status word (synchronises the stream).
+fjg_status take_status(fjg_ctx* ctx, cudaStream_t s) {
+  int st = 0;
+  cudaError_t err = cudaMemcpyAsync(&st, ctx->sc.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "clustering");
+  if (st) {
+    cudaMemsetAsync(ctx->sc.status, 0, sizeof(int), s);
+    cudaStreamSynchronize(s);
+    if (st & fjg::kStatusTooBig)
+      return set_error(ctx, FJG_ETOOBIG, "an event exceeds the supported particle count");
+    if (st & fjg::kStatusInternal)
+      return set_error(ctx, FJG_EKERNEL, "a clustering kernel found no candidate (non-finite input?)");
+    return set_error(ctx, FJG_EINVAL, "invalid event offsets");
+  }
+  return FJG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fjg_status_string(fjg_status s) {
+  switch (s) {
+    case FJG_OK: return "ok";
+    case FJG_EINVAL: return "invalid argument";
+    case FJG_ENOMEM: return "out of memory";
+    case FJG_ECUDA: return "CUDA error";
+    case FJG_ETOOBIG: return "event too large";
+    case FJG_ETIMEDOUT: return "timed out";
+    case FJG_EAGAIN: return "try again";
+    case FJG_EKERNEL: return "kernel error";
+  }
+  return "unknown status";
+}
+
+const char* fjg_last_error(const fjg_ctx* ctx) { return ctx ? ctx->last_error.c_str() : g_thread_error.c_str(); }
+
+fjg_status fjg_ctx_create(int device, fjg_ctx** out) {
+  if (!out) return set_error(nullptr, FJG_EINVAL, "out is null");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t err = cudaGetDeviceCount(&count);
+  if (err != cudaSuccess) return cuda_error(nullptr, err, "cudaGetDeviceCount");
+  if (device < 0 || device >= count) return set_error(nullptr, FJG_EINVAL, "no such CUDA device");
+  fjg_ctx* ctx = new (std::nothrow) fjg_ctx();
+  if (!ctx) return set_error(nullptr, FJG_ENOMEM, "host allocation failed");
+  ctx->device = device;
+  DeviceGuard g(device);
+  err = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  for (int b = 0; b < fjg::kNumBuckets && err == cudaSuccess; ++b) {
+    err = cudaStreamCreateWithFlags(&ctx->side[b], cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ctx->ev_join[b], cudaEventDisableTiming);
+  }
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+  if (err == cudaSuccess) err = ensure_scratch(ctx, 1024);
+  if (err != cudaSuccess) {
+    fjg_status st = cuda_error(nullptr, err, "context creation");
+    fjg_ctx_destroy(ctx);
+    return st;
+  }
+  *out = ctx;
+  return FJG_OK;
+}
+
+void fjg_ctx_destroy(fjg_ctx* ctx) {
+  if (!ctx) return;
+  DeviceGuard g(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (int b = 0; b < fjg::kNumBuckets; ++b) {
+    if (ctx->side[b]) {
+      cudaStreamSynchronize(ctx->side[b]);
+      cudaStreamDestroy(ctx->side[b]);
+    }
+    if (ctx->ev_join[b]) cudaEventDestroy(ctx->ev_join[b]);
+  }
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  ctx->scratch.release();
+  ctx->io.release();
+  ctx->single.release();
+  delete ctx;
+}
+
+void* fjg_ctx_stream(fjg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+fjg_status fjg_ctx_check(fjg_ctx* ctx) {
+  if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
+  DeviceGuard g(ctx->device);
+  for (int b = 0; b < fjg::kNumBuckets; ++b) cudaStreamSynchronize(ctx->side[b]);
+  return take_status(ctx, ctx->stream);
+}
+
+fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offsets, int n_events, int64_t total,
+                             const int32_t* algo, int algo_all, const double* radius, double r_all,
+                             const fjg_outputs* out, void* stream) {
+  if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
+  if (n_events < 0 || total < 0 || !offsets || !out || !out->n_jets) return set_error(ctx, FJG_EINVAL, "bad batch arguments");
+  if (n_events == 0) return FJG_OK;
+  if (total > 0 && (!p4 || !out->jets || !out->jet_label)) return set_error(ctx, FJG_EINVAL, "null buffer");
+  if (!algo && !valid_algo(algo_all)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
+  if (!radius && !(r_all > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  DeviceGuard g(ctx->device);
+  cudaError_t err = ensure_scratch(ctx, n_events);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "scratch allocation");
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  BatchArgs A{};
+  A.p4 = p4;
+  A.p4_stride = 4;
+  A.offsets = offsets;
+  A.algo = algo;
+  A.radius = radius;
+  A.algo_all = algo_all;
+  A.r_all = r_all;
+  A.jets = out->jets;
+  A.jet_label = out->jet_label;
+  A.n_jets = out->n_jets;
+  A.history = reinterpret_cast<fjg::StepRec*>(out->history);
+  A.owner = out->owner;
+  A.status = ctx->sc.status;
+  err = fjg::launch_batch(A, ctx->sc, n_events, ctx->num_sms, s, ctx->side, &ctx->ev_fork, ctx->ev_join);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "batch launch");
+  return FJG_OK;
+}
+
+fjg_status fjg_cluster_batch_host(fjg_ctx* ctx, const double* p4, const int64_t* offsets, int n_events,
+                                  const int32_t* algo, int algo_all, const double* radius, double r_all,
+                                  const fjg_outputs* out) {
+  if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
+  if (n_events < 0 || !offsets || !out || !out->n_jets) return set_error(ctx, FJG_EINVAL, "bad batch arguments");
+  if (n_events == 0) return FJG_OK;
+  const int64_t total = offsets[n_events];
+  if (offsets[0] != 0 || total < 0) return set_error(ctx, FJG_EINVAL, "offsets must start at 0");
+  for (int e = 0; e < n_events; ++e)
+    if (offsets[e + 1] < offsets[e]) return set_error(ctx, FJG_EINVAL, "offsets must be non-decreasing");
+  if (total > 0 && (!p4 || !out->jets || !out->jet_label)) return set_error(ctx, FJG_EINVAL, "null buffer");
+  DeviceGuard g(ctx->device);
+  // device layout: p4 | offsets | algo | radius | jets | labels | n_jets | history | owner
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t b_p4 = al(sizeof(double) * 4 * total), b_off = al(sizeof(int64_t) * (n_events + 1));
+  const size_t b_algo = algo ? al(sizeof(int32_t) * n_events) : 0, b_rad = radius ? al(sizeof(double) * n_events) : 0;
+  const size_t b_jets = al(sizeof(double) * 4 * total), b_lab = al(sizeof(int32_t) * total);
+  const size_t b_nj = al(sizeof(int32_t) * n_events);
+  const size_t b_hist = out->history ? al(sizeof(fjg_step) * total) : 0;
+  const size_t b_own = out->owner ? al(sizeof(int32_t) * total) : 0;
+  cudaError_t err = ctx->io.reserve(b_p4 + b_off + b_algo + b_rad + b_jets + b_lab + b_nj + b_hist + b_own);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "device buffers");
+  char* d = static_cast<char*>(ctx->io.ptr);
+  double* d_p4 = reinterpret_cast<double*>(d);
+  d += b_p4;
+  int64_t* d_off = reinterpret_cast<int64_t*>(d);
+  d += b_off;
+  int32_t* d_algo = algo ? reinterpret_cast<int32_t*>(d) : nullptr;
+  d += b_algo;
+  double* d_rad = radius ? reinterpret_cast<double*>(d) : nullptr;
+  d += b_rad;
+  fjg_outputs dout{};
+  dout.jets = reinterpret_cast<double*>(d);
+  d += b_jets;
+  dout.jet_label = reinterpret_cast<int32_t*>(d);
+  d += b_lab;
+  dout.n_jets = reinterpret_cast<int32_t*>(d);
+  d += b_nj;
+  dout.history = out->history ? reinterpret_cast<fjg_step*>(d) : nullptr;
+  d += b_hist;
+  dout.owner = out->owner ? reinterpret_cast<int32_t*>(d) : nullptr;
+  cudaStream_t s = ctx->stream;
+  err = cudaMemcpyAsync(d_p4, p4, sizeof(double) * 4 * total, cudaMemcpyHostToDevice, s);
+  if (err == cudaSuccess) err = cudaMemcpyAsync(d_off, offsets, sizeof(int64_t) * (n_events + 1), cudaMemcpyHostToDevice, s);
+  if (err == cudaSuccess && algo) err = cudaMemcpyAsync(d_algo, algo, sizeof(int32_t) * n_events, cudaMemcpyHostToDevice, s);
+  if (err == cudaSuccess && radius) err = cudaMemcpyAsync(d_rad, radius, sizeof(double) * n_events, cudaMemcpyHostToDevice, s);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "input copy");
+  fjg_status st = fjg_cluster_batch(ctx, d_p4, d_off, n_events, total, d_algo, algo_all, d_rad, r_all, &dout, s);
+  if (st != FJG_OK) return st;
+  err = cudaMemcpyAsync(out->n_jets, dout.n_jets, sizeof(int32_t) * n_events, cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaMemcpyAsync(out->jets, dout.jets, sizeof(double) * 4 * total, cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaMemcpyAsync(out->jet_label, dout.jet_label, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess && out->history)
+    err = cudaMemcpyAsync(out->history, dout.history, sizeof(fjg_step) * total, cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess && out->owner)
+    err = cudaMemcpyAsync(out->owner, dout.owner, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, s);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "output copy");
+  return take_status(ctx, s);
+}
+
+fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, double r, double* jets,
+                             int32_t* jet_label, int32_t* n_jets, fjg_step* history, int32_t* owner) {
+  if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
+  if (n < 0 || !n_jets || (n > 0 && (!p4 || !jets || !jet_label))) return set_error(ctx, FJG_EINVAL, "bad arguments");
+  if (!valid_algo(algo)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
+  if (!(r > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = ctx->stream;
+  if (n == 0) {
+    cudaError_t err = cudaMemsetAsync(n_jets, 0, sizeof(int32_t), s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    return err == cudaSuccess ? FJG_OK : cuda_error(ctx, err, "fjg_cluster_event");
+  }
+  if (n > fjg::kSmemMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the per-event path's particle limit");
+  BatchArgs A{};
+  A.p4 = p4;
+  A.p4_stride = 4;
+  A.algo = nullptr;
+  A.radius = nullptr;
+  A.algo_all = algo;
+  A.r_all = r;
+  A.jets = jets;
+  A.jet_label = jet_label;
+  A.n_jets = n_jets;
+  A.history = reinterpret_cast<fjg::StepRec*>(history);
+  A.owner = owner;
+  A.status = ctx->sc.status;
+  cudaError_t err = fjg::launch_single(A, ctx->sc, n, s);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "fjg_cluster_event launch");
+  return take_status(ctx, s);
+}
+
+fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int size, int algo, double r,
+                                  void* stream) {
+  if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
+  if (size < 0 || (size > 0 && !particles)) return set_error(ctx, FJG_EINVAL, "bad arguments");
+  if (!valid_algo(algo)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
+  if (!(r > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  if (size == 0) return FJG_OK;
+  if (size > fjg::kSmemMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the supported particle count");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t b_jets = al(sizeof(double) * 4 * size), b_lab = al(sizeof(int32_t) * size);
+  cudaError_t err = ctx->single.reserve(b_jets + b_lab + 256);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "device buffers");
+  char* d = static_cast<char*>(ctx->single.ptr);
+  double* jets = reinterpret_cast<double*>(d);
+  int32_t* labels = reinterpret_cast<int32_t*>(d + b_jets);
+  int32_t* nj = reinterpret_cast<int32_t*>(d + b_jets + b_lab);
+  BatchArgs A{};
+  // px of record s sits 8 bytes into the 40-byte record: a stride of 5 doubles
+  A.p4 = reinterpret_cast<const double*>(reinterpret_cast<const char*>(particles) + 8);
+  A.p4_stride = 5;
+  A.algo_all = algo;
+  A.r_all = r;
+  A.jets = jets;
+  A.jet_label = labels;
+  A.n_jets = nj;
+  A.status = ctx->sc.status;
+  err = fjg::launch_single(A, ctx->sc, size, s);
+  if (err == cudaSuccess) err = fjg::launch_pseudojet_epilogue(particles, size, jets, labels, nj, s);
+  if (err != cudaSuccess) return cuda_error(ctx, err, "fjg_cluster_pseudojets");
+  return take_status(ctx, s);
+}
+
+}  // extern "C"

@@ -225,7 +225,11 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       Arg x = (lane < W) ? S.warg[lane] : Arg{~0ull, 0x7fffffff, -1};
       x = arg_warp(x.key, x.label, x.idx);
       // 2. promote or merge (thread 0)
-      if (tid == 0) {
+      if (tid == 0 && x.idx < 0) {
+        // no candidate although n > 0: cannot happen for finite inputs; stop this event
+        atomicOr(A.status, 4);
+        S.ctl_pair = -1;
+      } else if (tid == 0) {
         const int s = x.idx;
         const double key = S.key[s];
         const int L = n - 1;
@@ -292,6 +296,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       }
     }
     __syncthreads();  // B2
+    if (S.ctl_pair < 0) break;
     --n;
     ++step;
     const int a = S.ctl_a, b = S.ctl_b, L = S.ctl_L;

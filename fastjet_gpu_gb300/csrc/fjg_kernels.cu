@@ -1,0 +1,186 @@
+// Persistent clustering kernels (one per size bucket) and the bucketing pass.
+#include "fjg_kernels.cuh"
+
+namespace fjg {
+
+template <int T, int SPT>
+__global__ void __launch_bounds__(T) k_cluster_smem(BatchArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemLayout<T, SPT>& S = *reinterpret_cast<SmemLayout<T, SPT>*>(smem_raw);
+  const int count = *A.n_order;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int q = atomicAdd(A.queue, 1);
+      S.event = (q < count) ? A.order[q] : -1;
+    }
+    __syncthreads();
+    const int e = S.event;
+    if (e < 0) break;
+    cluster_event_smem<T, SPT>(S, A, e);  // ends with a barrier
+  }
+}
+
+// Distribute events into size buckets; empty events are finished here.
+__global__ void k_bucket(const int64_t* offsets, int n_events, int32_t* order, int32_t* counts, int cap_events,
+                         int32_t* n_jets, int* status) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
+    const int64_t n64 = offsets[e + 1] - offsets[e];
+    if (n64 < 0) {
+      atomicOr(status, kStatusBadArg);
+      n_jets[e] = 0;
+      continue;
+    }
+    if (n64 == 0) {
+      n_jets[e] = 0;
+      continue;
+    }
+    const int b = (n64 > kSmemMaxN) ? -1 : bucket_of((int)n64);
+    if (b < 0) {
+      atomicOr(status, kStatusTooBig);
+      n_jets[e] = 0;
+      continue;
+    }
+    const int pos = atomicAdd(&counts[b], 1);
+    order[b * cap_events + pos] = e;
+  }
+}
+
+template <int T, int SPT>
+static cudaError_t launch_bucket(const BatchArgs& A, int grid, cudaStream_t s) {
+  const size_t smem = sizeof(SmemLayout<T, SPT>);
+  // the attribute is per device: set it once for each device this process uses
+  static bool configured[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || !configured[dev]) {
+    cudaError_t err = cudaFuncSetAttribute(k_cluster_smem<T, SPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+    if (err != cudaSuccess) return err;
+    if (dev >= 0 && dev < 64) configured[dev] = true;
+  }
+  k_cluster_smem<T, SPT><<<grid, T, smem, s>>>(A);
+  return cudaGetLastError();
+}
+
+template <int T, int SPT>
+static int blocks_per_sm() {
+  int nb = 0;
+  const size_t smem = sizeof(SmemLayout<T, SPT>);
+  cudaFuncSetAttribute(k_cluster_smem<T, SPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cluster_smem<T, SPT>, T, smem) != cudaSuccess) nb = 1;
+  return nb < 1 ? 1 : nb;
+}
+
+static cudaError_t launch_bucket_dispatch(int b, const BatchArgs& A, int grid, cudaStream_t s) {
+  switch (b) {
+    case 0: return launch_bucket<64, 4>(A, grid, s);
+    case 1: return launch_bucket<128, 4>(A, grid, s);
+    case 2: return launch_bucket<256, 4>(A, grid, s);
+    default: return launch_bucket<512, 4>(A, grid, s);
+  }
+}
+
+static int bucket_blocks_per_sm(int b) {
+  static int cache[kNumBuckets] = {0, 0, 0, 0};
+  if (cache[b] == 0) {
+    switch (b) {
+      case 0: cache[b] = blocks_per_sm<64, 4>(); break;
+      case 1: cache[b] = blocks_per_sm<128, 4>(); break;
+      case 2: cache[b] = blocks_per_sm<256, 4>(); break;
+      default: cache[b] = blocks_per_sm<512, 4>(); break;
+    }
+  }
+  return cache[b];
+}
+
+cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
+                         cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join) {
+  cudaError_t err;
+  if ((err = cudaMemsetAsync(sc.counts, 0, sizeof(int32_t) * kNumBuckets, stream)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumBuckets, stream)) != cudaSuccess) return err;
+  const int bgrid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
+  k_bucket<<<bgrid, 256, 0, stream>>>(base.offsets, n_events, sc.order, sc.counts, sc.cap_events, base.n_jets,
+                                      sc.status);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  if ((err = cudaEventRecord(*ev_fork, stream)) != cudaSuccess) return err;
+  // largest events first: their bucket is launched first
+  for (int b = kNumBuckets - 1; b >= 0; --b) {
+    cudaStream_t s = side ? side[b] : stream;
+    if (side && (err = cudaStreamWaitEvent(s, *ev_fork, 0)) != cudaSuccess) return err;
+    BatchArgs A = base;
+    A.order = sc.order + b * sc.cap_events;
+    A.n_order = sc.counts + b;
+    A.queue = sc.queues + b;
+    int grid = num_sms * bucket_blocks_per_sm(b);
+    if (grid > n_events) grid = n_events;
+    if (grid < 1) grid = 1;
+    if ((err = launch_bucket_dispatch(b, A, grid, s)) != cudaSuccess) return err;
+    if (side) {
+      if ((err = cudaEventRecord(ev_join[b], s)) != cudaSuccess) return err;
+      if ((err = cudaStreamWaitEvent(stream, ev_join[b], 0)) != cudaSuccess) return err;
+    }
+  }
+  return cudaSuccess;
+}
+
+__global__ void k_single_setup(int64_t* offsets1, int32_t* order, int32_t* counts, int* queues, int n) {
+  offsets1[0] = 0;
+  offsets1[1] = n;
+  order[0] = 0;
+  for (int b = 0; b < kNumBuckets; ++b) {
+    counts[b] = 1;
+    queues[b] = 0;
+  }
+}
+
+cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream) {
+  const int b = bucket_of(n);
+  if (b < 0) return cudaErrorInvalidValue;
+  k_single_setup<<<1, 1, 0, stream>>>(sc.offsets1, sc.order, sc.counts, sc.queues, n);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  BatchArgs A = base;
+  A.offsets = sc.offsets1;
+  A.order = sc.order;
+  A.n_order = sc.counts;
+  A.queue = sc.queues;
+  return launch_bucket_dispatch(b, A, 1, stream);
+}
+
+// PseudoJet record (PseudoJet.h:4-11): int index; bool isJet; double px, py, pz, E.
+struct PJRecord {
+  int index;
+  bool isJet;
+  double px, py, pz, E;
+};
+static_assert(sizeof(PJRecord) == 40, "PseudoJet layout");
+
+__global__ void k_pj_reset(PJRecord* rec, int size) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < size; s += gridDim.x * blockDim.x) {
+    rec[s].index = s;
+    rec[s].isJet = false;
+  }
+}
+
+__global__ void k_pj_scatter(PJRecord* rec, const double* jets, const int32_t* jet_label, const int32_t* n_jets) {
+  const int nj = *n_jets;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nj; k += gridDim.x * blockDim.x) {
+    const int s = jet_label[k];
+    rec[s].px = jets[4 * k + 0];
+    rec[s].py = jets[4 * k + 1];
+    rec[s].pz = jets[4 * k + 2];
+    rec[s].E = jets[4 * k + 3];
+    rec[s].isJet = true;
+  }
+}
+
+cudaError_t launch_pseudojet_epilogue(void* records, int size, const double* jets, const int32_t* jet_label,
+                                      const int32_t* n_jets, cudaStream_t stream) {
+  if (size <= 0) return cudaSuccess;
+  const int grid = (size + 255) / 256 > 256 ? 256 : (size + 255) / 256;
+  k_pj_reset<<<grid, 256, 0, stream>>>(reinterpret_cast<PJRecord*>(records), size);
+  k_pj_scatter<<<grid, 256, 0, stream>>>(reinterpret_cast<PJRecord*>(records), jets, jet_label, n_jets);
+  return cudaGetLastError();
+}
+
+}  // namespace fjg

@@ -1,0 +1,46 @@
+// Kernel entry points and launch helpers shared by the C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fjg_cluster.cuh"
+
+namespace fjg {
+
+// Size buckets of the shared-memory path: capacity C = threads * 4 slots.
+constexpr int kNumBuckets = 4;
+constexpr int kSmemMaxN = 2048;
+
+// bucket b holds events of up to 256 << b particles, run by CTAs of 64 << b threads
+__host__ __device__ inline int bucket_of(int n) {
+  return n <= 256 ? 0 : n <= 512 ? 1 : n <= 1024 ? 2 : n <= 2048 ? 3 : -1;
+}
+
+// Status bits raised by kernels (ORed into the device status word).
+enum : int { kStatusTooBig = 1, kStatusBadArg = 2, kStatusInternal = 4 };
+
+static_assert(sizeof(SmemLayout<512, 4>) <= 232448, "bucket 3 exceeds the opt-in shared memory per block");
+
+// Device-side batch descriptor scratch owned by a context.
+struct Scratch {
+  int32_t* order;   // [kNumBuckets][cap_events]
+  int32_t* counts;  // [kNumBuckets]
+  int* queues;      // [kNumBuckets]
+  int* status;      // [1]
+  int64_t* offsets1;  // [2] single-event offsets {0, n}
+  int cap_events;
+};
+
+// Launch the bucketing kernel plus one persistent kernel per bucket on
+// `stream` (buckets run concurrently on the side streams when given).
+cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
+                         cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join);
+
+// One event, one CTA (the plain per-event-launch path).
+cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream);
+
+// Scatter jets into the reference's PseudoJet records (in place).
+cudaError_t launch_pseudojet_epilogue(void* records, int size, const double* jets, const int32_t* jet_label,
+                                      const int32_t* n_jets, cudaStream_t stream);
+
+}  // namespace fjg

@@ -50,7 +50,11 @@ typedef enum {
 /* I/O record of the reference (PseudoJet.h:4-11): 40 bytes, px at offset 8. */
 typedef struct {
   int index;
+#ifdef __cplusplus
+  bool isJet;
+#else
   _Bool isJet;
+#endif
   double px, py, pz, E;
 } fjg_pseudojet;
 
@@ -84,6 +88,9 @@ void fjg_ctx_destroy(fjg_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t). */
 void* fjg_ctx_stream(fjg_ctx* ctx);
 const char* fjg_status_string(fjg_status s);
+/* Wait for the context's work and report (then clear) errors raised by its
+ * kernels since the last check, e.g. FJG_ETOOBIG from an asynchronous batch. */
+fjg_status fjg_ctx_check(fjg_ctx* ctx);
 /* Last error message of the context (or of the calling thread when ctx is NULL). */
 const char* fjg_last_error(const fjg_ctx* ctx);
 

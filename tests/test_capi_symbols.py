@@ -1,0 +1,59 @@
+"""The C-ABI library builds for sm_103a and exports every symbol its headers declare.
+
+No compute calls: this runs without a GPU.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from fastjet_gpu_gb300 import build as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    names = set()
+    for h in ("fastjet_gb300.h",):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(fjg_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    return B.build()
+
+
+def test_exports_every_declared_symbol(libpath):
+    L = ctypes.CDLL(libpath)
+    names = _declared_functions()
+    assert "fjg_cluster_batch" in names and "fjg_cluster_pseudojets" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_exports_reference_cpp_symbol(libpath):
+    # cluster(PseudoJet*, int, Algorithm, double) from cluster.h:6
+    out = subprocess.run(["nm", "-D", "--defined-only", libpath], capture_output=True, text=True, check=True).stdout
+    assert "_Z7clusterP9PseudoJeti9Algorithmd" in out
+
+
+def test_status_strings(libpath):
+    L = ctypes.CDLL(libpath)
+    L.fjg_status_string.restype = ctypes.c_char_p
+    assert L.fjg_status_string(0) == b"ok"
+    assert L.fjg_status_string(4) == b"event too large"
+
+
+def test_compat_header_matches_reference_layout():
+    # PseudoJet.h:4-11 layout: 40 bytes, px at offset 8
+    import numpy as np
+    import fastjet_gpu_gb300 as F
+    assert F.PSEUDOJET.itemsize == 40
+    assert F.PSEUDOJET.fields["px"][1] == 8 and F.PSEUDOJET.fields["E"][1] == 32
+    assert int(F.Algorithm.Kt) == 1 and int(F.Algorithm.CambridgeAachen) == 0 and int(F.Algorithm.AntiKt) == -1

@@ -1,0 +1,162 @@
+"""GPU clustering vs the reference goldens and the CPU oracle (needs a GB300)."""
+import collections
+
+import numpy as np
+import pytest
+
+import golden_util as G
+import gpu_util as U
+from fastjet_gpu_gb300 import events as E
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fastjet_gpu_gb300 as F
+    return F.Context(0)
+
+
+def _batch(evs):
+    b = E._batch_from(evs)
+    return b.particles, b.offsets
+
+
+def test_reference_goldens_bit_exact(ctx):
+    """Every reference golden case (552): identical jet sets, bit for bit."""
+    by = collections.defaultdict(list)
+    for case in G.cases():
+        by[(case[0], case[1], case[2])].append(case)
+    n = 0
+    for (name, algo, radius), cs in sorted(by.items()):
+        evs = G.inputs(name)
+        p4, off = _batch(evs)
+        res = ctx.cluster_batch(p4, off, G.ALGO_CODE[algo], float(radius))
+        for _, _, _, ev, nj, dg in cs:
+            got = res["n_jets"][ev]
+            assert got == nj, (name, algo, radius, ev)
+            jets = res["jets"][off[ev]:off[ev] + got]
+            assert G.jets_digest(jets) == dg, (name, algo, radius, ev)
+            n += 1
+    assert n == 552
+
+
+@pytest.mark.parametrize("algo", [1, 0, -1])
+@pytest.mark.parametrize("radius", [0.4, 0.8, 1.0])
+def test_history_matches_oracle(ctx, algo, radius):
+    b = E.mixed_batch(40, 2, 2048, seed=21 + algo)
+    res = ctx.cluster_batch(b.particles, b.offsets, algo, radius, history=True, owner=True)
+    for e in range(b.n_events):
+        o0, o1 = b.offsets[e], b.offsets[e + 1]
+        U.compare_event(b.event(e), algo, radius, res["jets"][o0:o1], res["n_jets"][e], res["history"][o0:o1],
+                        res["owner"][o0:o1], res["jet_label"][o0:o1], ctx=f"event {e} n={o1 - o0}")
+
+
+def test_bucket_boundaries_and_tiny(ctx):
+    sizes = [0, 1, 2, 3, 31, 32, 33, 255, 256, 257, 511, 512, 513, 1023, 1024, 1025, 2047, 2048]
+    evs = [E.single_event(n, 2, seed=n) if n else np.zeros((0, 4)) for n in sizes]
+    p4, off = _batch(evs)
+    for algo in (1, 0, -1):
+        res = ctx.cluster_batch(p4, off, algo, 0.6, history=True, owner=True)
+        for e, n in enumerate(sizes):
+            o0, o1 = off[e], off[e + 1]
+            U.compare_event(evs[e], algo, 0.6, res["jets"][o0:o1], res["n_jets"][e], res["history"][o0:o1],
+                            res["owner"][o0:o1], ctx=f"n={n} algo={algo}")
+
+
+def test_mixed_algorithms_and_radii_per_event(ctx):
+    b, algo, radius = E.serving_mix(60, seed=8, hi=2000)
+    res = ctx.cluster_batch(b.particles, b.offsets, algo, radius, history=True)
+    for e in range(b.n_events):
+        o0, o1 = b.offsets[e], b.offsets[e + 1]
+        U.compare_event(b.event(e), int(algo[e]), float(radius[e]), res["jets"][o0:o1], res["n_jets"][e],
+                        res["history"][o0:o1], ctx=f"event {e}")
+
+
+def _symmetric_ladder(k=12):
+    """A particle at rapidity 0 between mirrored particles at +-rap_i (phi = 0):
+    dR2 to the left and right neighbours tie exactly, whatever the libm."""
+    rows = [[1.0, 0.0, 0.0, 1.0]]
+    for i in range(1, k + 1):
+        s = 0.05 * i ** 1.3
+        e = float(np.sqrt(1.0 + s * s))
+        rows.append([1.0, 0.0, s, e])
+        rows.append([1.0, 0.0, -s, e])
+    return np.array(rows)
+
+
+def test_degenerate_inputs(ctx):
+    """Ties and special branches whose resolution does not depend on the last
+    bits of log/atan2 (those would differ between CUDA's and the host's libm)."""
+    zero_pt = np.array([[0.0, 0.0, 5.0, 5.0], [0.0, 0.0, -3.0, 3.0], [1.0, 0.5, 0.2, 1.2], [0.9, 0.6, 0.1, 1.1],
+                        [0.0, 0.0, 0.0, 0.0], [0.0, 0.0, 2.0, 7.0]])
+    # widely separated particles: every step promotes (C/A: all at d = 1, lowest label first)
+    ring = np.array([[np.cos(t), np.sin(t), 0.0, 1.0] for t in np.linspace(0, 6, 40)])
+    dup = np.repeat(E.single_event(20, 1, seed=5), 2, axis=0)  # exact duplicates: dR2 == 0 ties
+    massive = E.single_event(300, 3, seed=6)
+    massive[:, 3] *= 1.3  # E > |p|
+    ladder = _symmetric_ladder()
+    cases = [(zero_pt, (0.05, 0.7)), (ring, (0.05,)), (dup, (0.05, 0.7)), (massive, (0.05, 0.7)),
+             (ladder, (0.3, 1.0))]
+    for algo in (1, 0, -1):
+        for ci, (ev, radii) in enumerate(cases):
+            for radius in radii:
+                res = ctx.cluster_batch(ev, np.array([0, ev.shape[0]]), algo, radius, history=True, owner=True)
+                U.compare_event(ev, algo, radius, res["jets"], res["n_jets"][0], res["history"], res["owner"],
+                                ctx=f"case {ci} algo {algo} R {radius}")
+
+
+def test_batch_invariance_and_determinism(ctx):
+    b = E.mixed_batch(64, 50, 2000, seed=31)
+    r1 = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, history=True)
+    r2 = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, history=True)
+    for k in ("jets", "jet_label", "n_jets", "history"):
+        assert np.array_equal(r1[k], r2[k])
+    for e in (0, 7, 63):
+        ev = b.event(e)
+        alone = ctx.cluster_batch(ev, np.array([0, ev.shape[0]]), -1, 0.4, history=True)
+        o0, o1 = b.offsets[e], b.offsets[e + 1]
+        assert np.array_equal(alone["jets"][:alone["n_jets"][0]], r1["jets"][o0:o0 + r1["n_jets"][e]])
+        assert np.array_equal(alone["history"], r1["history"][o0:o1])
+
+
+def test_plain_path_matches_batch(ctx):
+    import torch
+    b = E.mixed_batch(6, 50, 2000, seed=41)
+    r = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, history=True)
+    for e in range(b.n_events):
+        ev = torch.from_numpy(b.event(e)).cuda()
+        one = ctx.cluster_event(ev, -1, 0.4, history=True)
+        nj = int(one["n_jets"][0])
+        o0 = b.offsets[e]
+        assert nj == r["n_jets"][e]
+        assert np.array_equal(one["jets"][:nj].cpu().numpy(), r["jets"][o0:o0 + nj])
+
+
+def test_pseudojet_records_in_place(ctx):
+    """cluster.h:6 contract on PseudoJet records: jets flagged isJet at their label slot."""
+    import fastjet_gpu_gb300 as F
+    import oracle
+    ev = G.inputs("808_cms")[0]
+    rec = np.zeros(ev.shape[0], F.PSEUDOJET)
+    rec["index"] = np.arange(ev.shape[0])
+    rec["px"], rec["py"], rec["pz"], rec["E"] = ev.T
+    ctx.cluster_pseudojets(rec, ev.shape[0], F.Algorithm.AntiKt, 0.4)
+    ref = oracle.cluster(ev, -1, 0.4)
+    assert rec["isJet"].sum() == len(ref.jets)
+    assert np.array_equal(np.flatnonzero(rec["isJet"]), np.sort(ref.jet_label))
+    got = np.stack([rec["px"], rec["py"], rec["pz"], rec["E"]], axis=1)[rec["isJet"]]
+    assert sorted(map(tuple, got.tolist())) == sorted(map(tuple, ref.jets.tolist()))
+    assert np.array_equal(rec["index"], np.arange(ev.shape[0]))
+
+
+def test_too_big_is_reported(ctx):
+    import fastjet_gpu_gb300 as F
+    ev = E.single_event(3000, 2, seed=1)
+    with pytest.raises(F.FjgError) as ei:
+        ctx.cluster_batch(ev, np.array([0, 3000]), -1, 0.4)
+    assert ei.value.status == 4
+    ctx.cluster_batch(ev[:100], np.array([0, 100]), -1, 0.4)  # the context stays usable
