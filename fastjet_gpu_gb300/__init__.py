@@ -78,6 +78,7 @@ def lib():
         L.fjg_cluster_batch_host.argtypes = [P, P, P, I, P, I, P, D, ctypes.POINTER(_Outputs)]
         L.fjg_cluster_event.argtypes = [P, P, I, I, D, P, P, P, P, P]
         L.fjg_cluster_pseudojets.argtypes = [P, P, I, I, D, P]
+        L.fjg_kinematics.argtypes = [P, P, I, I, P, P, P, P]
         _lib = L
     return _lib
 
@@ -209,6 +210,16 @@ class Context:
                                      _t_ptr(out.get("history")), _t_ptr(out.get("owner")))
         self._check(st)
         return out
+
+    def kinematics(self, p4, algo):
+        """(rap, phi, w) of device four-momenta (torch CUDA float64 [n, 4]), synchronous."""
+        import torch
+        n = p4.shape[0]
+        rap, phi, w = (torch.empty(max(n, 1), dtype=torch.float64, device=p4.device) for _ in range(3))
+        self._check(lib().fjg_kinematics(self._h, _t_ptr(p4), n, int(algo), _t_ptr(rap), _t_ptr(phi), _t_ptr(w),
+                                         None))
+        self.check()
+        return rap[:n], phi[:n], w[:n]
 
     def cluster_pseudojets(self, records, size, algo, radius):
         """In-place clustering of PseudoJet records (cluster.h:6 semantics).

@@ -323,6 +323,17 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
   return take_status(ctx, s);
 }
 
+fjg_status fjg_kinematics(fjg_ctx* ctx, const double* p4, int n, int algo, double* rap, double* phi, double* w,
+                          void* stream) {
+  if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
+  if (n < 0 || (n > 0 && (!p4 || !rap || !phi || !w))) return set_error(ctx, FJG_EINVAL, "bad arguments");
+  if (!valid_algo(algo)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  cudaError_t err = fjg::launch_kinematics(p4, n, algo, rap, phi, w, s);
+  return err == cudaSuccess ? FJG_OK : cuda_error(ctx, err, "fjg_kinematics");
+}
+
 fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int size, int algo, double r,
                                   void* stream) {
   if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");

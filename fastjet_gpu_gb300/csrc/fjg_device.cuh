@@ -1,12 +1,14 @@
 // Device primitives shared by the clustering kernels (sm_103a).
 //
 // Exactness contract.  Every value that takes part in a clustering decision
-// (rapidity, azimuth, weight, dR2, d_ij, d_iB) is computed in FP64 with the
+// (rapidity, azimuth, weight, dR2, d_ij, d_iB) is an FP64 value of the
 // reference's expressions (tri_matrix.cu:61-113, grid.cu:110-201), rounded
 // exactly as written: products and sums use __dmul_rn/__dadd_rn so that nvcc
-// cannot contract them into FMAs.  The CPU oracle is compiled with
-// -ffp-contract=off for the same reason; the two differ only where CUDA's and
-// the host libm's log/atan2 differ in the last place.
+// cannot contract them into FMAs, divisions are correctly rounded, and log /
+// atan2 come from fjg_kin.h (correctly rounded except within ~2^-12 ulp of a
+// rounding boundary).  The CPU oracle (compiled with -ffp-contract=off) agrees
+// bit for bit in its portable-kinematics form; its libm form differs only
+// where the host libm and fjg_kin.h round a log/atan2 differently.
 //
 // GB300 executes FP64 at a small fraction of its FP32 rate, so the O(n) scans
 // that look for nearest neighbours run in FP32 with a rigorous per-pair error
@@ -21,6 +23,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fjg_kin.h"
+
 namespace fjg {
 
 constexpr double kPi = 3.141592653589793238462643383279502884197;
@@ -34,27 +38,11 @@ struct Kin {
 };
 
 // Rapidity, azimuth and weight of a four-momentum (tri_matrix.cu:61-100;
-// weight per algorithm grid.cu:153-166, safe_inverse grid.cu:110).
+// weight per algorithm grid.cu:153-166, safe_inverse grid.cu:110), with the
+// logarithm, arctangent and divisions done in integer arithmetic (fjg_kin.h).
 __device__ __forceinline__ Kin kinematics(double px, double py, double pz, double E, int algo) {
   Kin k;
-  const double pt2 = __dadd_rn(__dmul_rn(px, px), __dmul_rn(py, py));
-  double phi = (pt2 == 0.0) ? 0.0 : atan2(py, px);
-  if (phi < 0.0) phi = __dadd_rn(phi, kTwoPi);
-  if (phi >= kTwoPi) phi = __dsub_rn(phi, kTwoPi);
-  double rap;
-  const double apz = fabs(pz);
-  if (E == apz && pt2 == 0.0) {
-    const double mr = __dadd_rn(kMaxRap, apz);
-    rap = (pz >= 0.0) ? mr : -mr;
-  } else {
-    const double m2 = fmax(0.0, __dsub_rn(__dmul_rn(__dadd_rn(E, pz), __dsub_rn(E, pz)), pt2));
-    const double epz = __dadd_rn(E, apz);
-    rap = __dmul_rn(0.5, log(__ddiv_rn(__dadd_rn(pt2, m2), __dmul_rn(epz, epz))));
-    if (pz > 0.0) rap = -rap;
-  }
-  k.rap = rap;
-  k.phi = phi;
-  k.w = (algo == 1) ? pt2 : (algo == 0) ? 1.0 : ((pt2 > 1e-300) ? __ddiv_rn(1.0, pt2) : 1e300);
+  fjk_kinematics(px, py, pz, E, algo, &k.rap, &k.phi, &k.w);
   return k;
 }
 

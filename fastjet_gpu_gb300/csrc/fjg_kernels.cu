@@ -147,6 +147,23 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaS
   return launch_bucket_dispatch(b, A, 1, stream);
 }
 
+__global__ void k_kinematics(const double* p4, int n, int algo, double* rap, double* phi, double* w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const Kin k = kinematics(p4[4 * i + 0], p4[4 * i + 1], p4[4 * i + 2], p4[4 * i + 3], algo);
+    rap[i] = k.rap;
+    phi[i] = k.phi;
+    w[i] = k.w;
+  }
+}
+
+cudaError_t launch_kinematics(const double* p4, int n, int algo, double* rap, double* phi, double* w,
+                              cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (n + 255) / 256 > 4096 ? 4096 : (n + 255) / 256;
+  k_kinematics<<<grid, 256, 0, stream>>>(p4, n, algo, rap, phi, w);
+  return cudaGetLastError();
+}
+
 // PseudoJet record (PseudoJet.h:4-11): int index; bool isJet; double px, py, pz, E.
 struct PJRecord {
   int index;

@@ -43,4 +43,9 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaS
 cudaError_t launch_pseudojet_epilogue(void* records, int size, const double* jets, const int32_t* jet_label,
                                       const int32_t* n_jets, cudaStream_t stream);
 
+// Rapidity, azimuth and weight of n four-momenta (the clustering kernels' own
+// kinematics routine, one thread per particle).
+cudaError_t launch_kinematics(const double* p4, int n, int algo, double* rap, double* phi, double* w,
+                              cudaStream_t stream);
+
 }  // namespace fjg

@@ -118,6 +118,13 @@ fjg_status fjg_cluster_batch_host(fjg_ctx* ctx, const double* p4, const int64_t*
 fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, double r, double* jets,
                              int32_t* jet_label, int32_t* n_jets, fjg_step* history, int32_t* owner);
 
+/* Rapidity, azimuth in [0, 2pi) and clustering weight (kt: pt^2, C/A: 1,
+ * anti-kt: 1/pt^2) of n device four-momenta, as the clustering kernels compute
+ * them; replaces the reference's per-particle _set_jet (tri_matrix.cu:61-100,
+ * grid.cu:112-171).  Asynchronous on `stream` (NULL: the context stream). */
+fjg_status fjg_kinematics(fjg_ctx* ctx, const double* p4, int n, int algo, double* rap, double* phi, double* w,
+                          void* stream);
+
 /* Drop-in for the reference's cluster() (cluster.h:6): `particles` is a device
  * buffer of `size` records, rewritten in place.  On return every record has
  * index = its input position; records whose slot holds a final jet have

@@ -40,6 +40,8 @@
 #include "fjg_oracle.h"
 
 #include <math.h>
+
+#include "fjg_kin.h"
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -81,6 +83,21 @@ void fjo_kinematics(const double p4[4], int algo, double* pt2_out, double* phi_o
 
 /* (d, l) ranks before (bd, bl): smaller distance, then smaller label */
 static inline int closer(double d, int32_t l, double bd, int32_t bl) { return d < bd || (d == bd && l < bl); }
+
+double fjo_kin_log(double x) { return fjk_log(x); }
+double fjo_kin_atan2(double y, double x) { return fjk_atan2(y, x); }
+double fjo_kin_div(double a, double b) { return fjk_div_rn(a, b); }
+void fjo_kin_kinematics(const double p4[4], int algo, double* rap, double* phi, double* w) {
+  fjk_kinematics(p4[0], p4[1], p4[2], p4[3], algo, rap, phi, w);
+}
+
+/* rapidity, azimuth and weight in the selected form (libm or portable) */
+static inline void kin(const double p[4], int algo, int portable, double* phi, double* rap, double* w) {
+  if (portable)
+    fjk_kinematics(p[0], p[1], p[2], p[3], algo, rap, phi, w);
+  else
+    fjo_kinematics(p, algo, NULL, phi, rap, w);
+}
 
 static inline double delta_r2(double rap1, double phi1, double rap2, double phi2) {
   double dphi = fabs(phi1 - phi2);
@@ -149,6 +166,8 @@ int fjo_cluster(const double* p4, int n, int algo, double R, int method, fjo_ste
                 int32_t* jet_label, int32_t* owner, int* n_jets_out, long long* pair_evals) {
   if (n < 0 || (n > 0 && !p4)) return -1;
   if (algo != FJO_KT && algo != FJO_CAM && algo != FJO_ANTIKT) return -1;
+  const int portable = (method & FJO_KIN_PORTABLE) != 0;
+  method &= ~FJO_KIN_PORTABLE;
   long long evals = 0;
   int n_jets = 0;
   if (n == 0) {
@@ -169,7 +188,7 @@ int fjo_cluster(const double* p4, int n, int algo, double R, int method, fjo_ste
 
   for (int s = 0; s < n; ++s) {
     memcpy(J[s].p, p4 + 4 * (size_t)s, sizeof(double) * 4);
-    fjo_kinematics(J[s].p, algo, NULL, &J[s].phi, &J[s].rap, &J[s].w);
+    kin(J[s].p, algo, portable, &J[s].phi, &J[s].rap, &J[s].w);
     J[s].label = s;
     J[s].nn = -1;
     J[s].nndist = INFINITY;
@@ -253,7 +272,7 @@ int fjo_cluster(const double* p4, int n, int algo, double R, int method, fjo_ste
       if (ri < rj) parent[rj] = ri; else parent[ri] = rj;
     }
     for (int c = 0; c < 4; ++c) J[i].p[c] = J[i].p[c] + J[j].p[c];
-    fjo_kinematics(J[i].p, algo, NULL, &J[i].phi, &J[i].rap, &J[i].w);
+    kin(J[i].p, algo, portable, &J[i].phi, &J[i].rap, &J[i].w);
     J[i].label = li < lj ? li : lj;
     {
       const int q = pos[j];
@@ -318,7 +337,8 @@ typedef struct {
   int32_t* n_jets;
   long long evals;
   int status;
-  int* next; /* shared work counter */
+  int kin_flag; /* FJO_KIN_PORTABLE or 0 */
+  int* next;    /* shared work counter */
   pthread_mutex_t* mu;
 } batch_task;
 
@@ -333,7 +353,7 @@ static void* batch_worker(void* arg) {
     const int n = (int)(t->offsets[e + 1] - o);
     int nj = 0;
     long long ev = 0;
-    const int rc = fjo_cluster(t->p4 + 4 * o, n, t->algo[e], t->R[e], FJO_NN_INCREMENTAL,
+    const int rc = fjo_cluster(t->p4 + 4 * o, n, t->algo[e], t->R[e], FJO_NN_INCREMENTAL | t->kin_flag,
                                t->history ? t->history + o : NULL, t->jets ? t->jets + 4 * o : NULL,
                                t->jet_label ? t->jet_label + o : NULL, t->owner ? t->owner + o : NULL, &nj, &ev);
     if (rc) t->status = rc;
@@ -346,6 +366,8 @@ static void* batch_worker(void* arg) {
 int fjo_cluster_batch(const double* p4, const int64_t* offsets, int n_events, const int32_t* algo,
                       const double* R, int threads, fjo_step* history, double* jets, int32_t* jet_label,
                       int32_t* owner, int32_t* n_jets, long long* pair_evals) {
+  const int kin_flag = (threads & FJO_KIN_PORTABLE << 16) ? FJO_KIN_PORTABLE : 0;
+  threads &= 0xffff;
   if (n_events < 0 || !offsets || !algo || !R) return -1;
   if (threads < 1) threads = 1;
   if (threads > 1024) threads = 1024;
@@ -362,7 +384,7 @@ int fjo_cluster_batch(const double* p4, const int64_t* offsets, int n_events, co
     batch_task* t = &tasks[k];
     t->p4 = p4; t->offsets = offsets; t->n_events = n_events; t->algo = algo; t->R = R;
     t->history = history; t->jets = jets; t->jet_label = jet_label; t->owner = owner; t->n_jets = n_jets;
-    t->next = &next; t->mu = &mu;
+    t->next = &next; t->mu = &mu; t->kin_flag = kin_flag;
   }
   int status = 0;
   for (int k = 1; k < threads; ++k)

@@ -28,6 +28,14 @@ enum { FJO_KT = 1, FJO_CAM = 0, FJO_ANTIKT = -1 };
  * nearest-neighbour recomputation at every step (O(N^3), a cross-check). */
 enum { FJO_NN_INCREMENTAL = 0, FJO_NN_RECOMPUTE = 1 };
 
+/* OR into `method`: compute rapidity/azimuth/weights with the library's
+ * integer kinematics (fastjet_gpu_gb300/csrc/fjg_kin.h) instead of the host
+ * libm.  The default (libm) form is the one pinned to the reference outputs;
+ * the portable form makes the oracle's arithmetic bit-identical to the CUDA
+ * kernels', so tests can demand exact equality even for ties that hinge on
+ * the last bit of log/atan2. */
+enum { FJO_KIN_PORTABLE = 16 };
+
 typedef struct {
   int32_t a;  /* label of the first pseudojet (the smaller label for a merge) */
   int32_t b;  /* label of the second pseudojet, or -1 when a is promoted to a jet */
@@ -38,6 +46,12 @@ typedef struct {
  * (tri_matrix.cu:61-100): pt2, phi in [0, 2pi), rapidity, and the weight w
  * (kt: pt2, C/A: 1, anti-kt: 1/pt2 guarded at 1e-300). */
 void fjo_kinematics(const double p4[4], int algo, double* pt2, double* phi, double* rap, double* w);
+
+/* The library's integer log / atan2 / division (fjg_kin.h), for tests. */
+double fjo_kin_log(double x);
+double fjo_kin_atan2(double y, double x);
+double fjo_kin_div(double a, double b);
+void fjo_kin_kinematics(const double p4[4], int algo, double* rap, double* phi, double* w);
 
 /* Cluster one event of n particles (p4: [n][4] px,py,pz,E).
  * Outputs (any may be NULL):
@@ -52,7 +66,8 @@ int fjo_cluster(const double* p4, int n, int algo, double R, int method, fjo_ste
                 int32_t* jet_label, int32_t* owner, int* n_jets, long long* pair_evals);
 
 /* Cluster a CSR batch (offsets[n_events+1]) with `threads` POSIX threads, one
- * event per task.  Outputs are CSR-indexed by the same offsets: history[total],
+ * event per task (threads | FJO_KIN_PORTABLE << 16 selects the portable
+ * kinematics).  Outputs are CSR-indexed by the same offsets: history[total],
  * jets[total][4], jet_label[total], owner[total]; n_jets[n_events].  Any output
  * may be NULL.  Returns 0 on success. */
 int fjo_cluster_batch(const double* p4, const int64_t* offsets, int n_events, const int32_t* algo,

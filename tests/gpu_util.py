@@ -6,8 +6,15 @@ import oracle
 D_RTOL = 1e-8  # history distances: see compare_event
 
 
-def compare_event(p4, algo, radius, jets, n_jets, history=None, owner=None, jet_label=None, ctx=""):
+def compare_event(p4, algo, radius, jets, n_jets, history=None, owner=None, jet_label=None, ctx="", portable=True):
     """Compare one event's GPU results with the CPU oracle.
+
+    portable=True (default): the oracle runs with the library's integer
+    kinematics (oracle.KIN_PORTABLE), i.e. the same FP64 values as the
+    kernels, so everything must be identical bit for bit, distances included
+    -- even for ties that hinge on the last bit of a log or atan2.
+    portable=False: the oracle's libm kinematics (the form pinned to the
+    reference outputs), compared as follows.
 
     Merge history: identical labels step by step (the merge decisions).  The
     recorded distances agree within 1e-8 relative: CUDA's and the host libm's
@@ -17,13 +24,17 @@ def compare_event(p4, algo, radius, jets, n_jets, history=None, owner=None, jet_
     bit-identical (same merge tree; an E-scheme sum of two pseudojets does not
     depend on their order), in the same promotion order.
     """
-    ref = oracle.cluster(p4, algo, radius)
+    method = oracle.NN_INCREMENTAL | (oracle.KIN_PORTABLE if portable else 0)
+    ref = oracle.cluster(p4, algo, radius, method)
     assert n_jets == len(ref.jets), f"{ctx}: n_jets {n_jets} vs {len(ref.jets)}"
     if history is not None:
         h = history
         assert np.array_equal(h["a"], ref.history["a"]) and np.array_equal(h["b"], ref.history["b"]), \
             f"{ctx}: merge history differs at step {int(np.flatnonzero((h['a'] != ref.history['a']) | (h['b'] != ref.history['b']))[0])}"
-        np.testing.assert_allclose(h["d"], ref.history["d"], rtol=D_RTOL, atol=0, err_msg=ctx)
+        if portable:
+            assert np.array_equal(h["d"], ref.history["d"]), f"{ctx}: distances differ"
+        else:
+            np.testing.assert_allclose(h["d"], ref.history["d"], rtol=D_RTOL, atol=0, err_msg=ctx)
     assert np.array_equal(jets[:n_jets], ref.jets), f"{ctx}: jets differ"
     if jet_label is not None:
         assert np.array_equal(jet_label[:n_jets], ref.jet_label), f"{ctx}: jet labels differ"

@@ -51,8 +51,10 @@ def test_history_matches_oracle(ctx, algo, radius):
     res = ctx.cluster_batch(b.particles, b.offsets, algo, radius, history=True, owner=True)
     for e in range(b.n_events):
         o0, o1 = b.offsets[e], b.offsets[e + 1]
-        U.compare_event(b.event(e), algo, radius, res["jets"][o0:o1], res["n_jets"][e], res["history"][o0:o1],
-                        res["owner"][o0:o1], res["jet_label"][o0:o1], ctx=f"event {e} n={o1 - o0}")
+        args = (b.event(e), algo, radius, res["jets"][o0:o1], res["n_jets"][e], res["history"][o0:o1],
+                res["owner"][o0:o1], res["jet_label"][o0:o1])
+        U.compare_event(*args, ctx=f"event {e} n={o1 - o0}")
+        U.compare_event(*args, ctx=f"libm: event {e} n={o1 - o0}", portable=False)
 
 
 def test_bucket_boundaries_and_tiny(ctx):
@@ -89,8 +91,9 @@ def _symmetric_ladder(k=12):
 
 
 def test_degenerate_inputs(ctx):
-    """Ties and special branches whose resolution does not depend on the last
-    bits of log/atan2 (those would differ between CUDA's and the host's libm)."""
+    """Exact ties and special branches.  Against the portable-kinematics oracle
+    every case must match bit for bit; against the libm oracle only the cases
+    whose tie resolution does not hinge on the last bit of log/atan2."""
     zero_pt = np.array([[0.0, 0.0, 5.0, 5.0], [0.0, 0.0, -3.0, 3.0], [1.0, 0.5, 0.2, 1.2], [0.9, 0.6, 0.1, 1.1],
                         [0.0, 0.0, 0.0, 0.0], [0.0, 0.0, 2.0, 7.0]])
     # widely separated particles: every step promotes (C/A: all at d = 1, lowest label first)
@@ -99,14 +102,17 @@ def test_degenerate_inputs(ctx):
     massive = E.single_event(300, 3, seed=6)
     massive[:, 3] *= 1.3  # E > |p|
     ladder = _symmetric_ladder()
-    cases = [(zero_pt, (0.05, 0.7)), (ring, (0.05,)), (dup, (0.05, 0.7)), (massive, (0.05, 0.7)),
-             (ladder, (0.3, 1.0))]
+    # (event, radii robust against libm differences, radii checked only bit-exactly)
+    cases = [(zero_pt, (0.05, 0.7), ()), (ring, (0.05,), (0.7, 1.0)), (dup, (0.05, 0.7), ()),
+             (massive, (0.05, 0.7), ()), (ladder, (0.3, 1.0), ())]
     for algo in (1, 0, -1):
-        for ci, (ev, radii) in enumerate(cases):
-            for radius in radii:
+        for ci, (ev, radii, exact_only) in enumerate(cases):
+            for radius in radii + exact_only:
                 res = ctx.cluster_batch(ev, np.array([0, ev.shape[0]]), algo, radius, history=True, owner=True)
-                U.compare_event(ev, algo, radius, res["jets"], res["n_jets"][0], res["history"], res["owner"],
-                                ctx=f"case {ci} algo {algo} R {radius}")
+                args = (ev, algo, radius, res["jets"], res["n_jets"][0], res["history"], res["owner"])
+                U.compare_event(*args, ctx=f"case {ci} algo {algo} R {radius}")
+                if radius in radii:
+                    U.compare_event(*args, ctx=f"libm: case {ci} algo {algo} R {radius}", portable=False)
 
 
 def test_batch_invariance_and_determinism(ctx):
