@@ -41,6 +41,8 @@ struct DeviceBuffer {
 
 }  // namespace
 
+void fjg::set_thread_error(const char* msg) { g_thread_error = msg; }
+
 struct fjg_ctx {
   int device = 0;
   int num_sms = 0;

@@ -123,6 +123,28 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
   return cudaSuccess;
 }
 
+cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
+                                   cudaStream_t stream) {
+  cudaError_t err;
+  if ((err = cudaMemsetAsync(sc.counts, 0, sizeof(int32_t) * kNumBuckets, stream)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumBuckets, stream)) != cudaSuccess) return err;
+  const int bgrid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
+  k_bucket<<<bgrid, 256, 0, stream>>>(base.offsets, n_events, sc.order, sc.counts, sc.cap_events, base.n_jets,
+                                      sc.status);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  for (int b = kNumBuckets - 1; b >= 0; --b) {
+    BatchArgs A = base;
+    A.order = sc.order + b * sc.cap_events;
+    A.n_order = sc.counts + b;
+    A.queue = sc.queues + b;
+    int grid = num_sms * bucket_blocks_per_sm(b);
+    if (grid > n_events) grid = n_events;
+    if (grid < 1) grid = 1;
+    if ((err = launch_bucket_dispatch(b, A, grid, stream)) != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
 __global__ void k_single_setup(int64_t* offsets1, int32_t* order, int32_t* counts, int* queues, int n) {
   offsets1[0] = 0;
   offsets1[1] = n;

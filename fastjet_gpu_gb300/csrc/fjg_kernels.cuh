@@ -36,6 +36,11 @@ struct Scratch {
 cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
                          cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join);
 
+// The bucketing kernel and the four bucket kernels, all on `stream` one after
+// another (no side streams, no events).
+cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
+                                   cudaStream_t stream);
+
 // One event, one CTA (the plain per-event-launch path).
 cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream);
 
@@ -47,5 +52,8 @@ cudaError_t launch_pseudojet_epilogue(void* records, int size, const double* jet
 // kinematics routine, one thread per particle).
 cudaError_t launch_kinematics(const double* p4, int n, int algo, double* rap, double* phi, double* w,
                               cudaStream_t stream);
+
+// Record a message as the calling thread's last error (fjg_last_error(NULL)).
+void set_thread_error(const char* msg);
 
 }  // namespace fjg
