@@ -54,6 +54,7 @@ struct fjg_ctx {
   DeviceBuffer scratch;  // order/counts/queues/status/offsets1
   DeviceBuffer io;       // device copies for the host-memory entry points
   DeviceBuffer single;   // outputs of fjg_cluster_pseudojets
+  DeviceBuffer wsbuf;    // exact per-particle state of the clustering kernels
   std::string last_error;
 };
 
@@ -90,7 +91,8 @@ cudaError_t ensure_scratch(fjg_ctx* ctx, int n_events) {
   if (n_events < 1) n_events = 1;
   if (ctx->sc.order && ctx->sc.cap_events >= n_events) return cudaSuccess;
   int cap = n_events + n_events / 4 + 64;
-  size_t bytes = sizeof(int32_t) * (size_t)fjg::kNumBuckets * cap + 64 * 4 + 64;
+  const size_t hist_bytes = (sizeof(int32_t) * fjg::kHistBins + 255) & ~size_t(255);
+  size_t bytes = sizeof(int32_t) * (size_t)fjg::kNumBuckets * cap + 256 + hist_bytes;
   cudaError_t err = ctx->scratch.reserve(bytes);
   if (err != cudaSuccess) return err;
   char* p = static_cast<char*>(ctx->scratch.ptr);
@@ -98,11 +100,24 @@ cudaError_t ensure_scratch(fjg_ctx* ctx, int n_events) {
   ctx->sc.counts = reinterpret_cast<int32_t*>(p + 64);
   ctx->sc.queues = reinterpret_cast<int*>(p + 128);
   ctx->sc.status = reinterpret_cast<int*>(p + 192);
-  ctx->sc.order = reinterpret_cast<int32_t*>(p + 256);
+  ctx->sc.hist = reinterpret_cast<int32_t*>(p + 256);
+  ctx->sc.order = reinterpret_cast<int32_t*>(p + 256 + hist_bytes);
   ctx->sc.cap_events = cap;
   err = cudaMemset(ctx->sc.status, 0, sizeof(int));
   if (err == cudaSuccess) err = cudaDeviceSynchronize();
   return err;
+}
+
+// Ensure the kernels' per-particle workspace holds `particles` entries.
+cudaError_t ensure_ws(fjg_ctx* ctx, int64_t particles) {
+  if (particles < 1) particles = 1;
+  if (ctx->sc.ws && ctx->sc.ws_stride >= particles) return cudaSuccess;
+  const int64_t stride = particles + particles / 4 + 1024;
+  cudaError_t err = ctx->wsbuf.reserve(sizeof(double) * fjg::kWsFields * (size_t)stride);
+  if (err != cudaSuccess) return err;
+  ctx->sc.ws = static_cast<double*>(ctx->wsbuf.ptr);
+  ctx->sc.ws_stride = (int64_t)(ctx->wsbuf.cap / (sizeof(double) * fjg::kWsFields));
+  return cudaSuccess;
 }
 
 bool valid_algo(int a) { return a == FJG_KT || a == FJG_CAM || a == FJG_ANTIKT; }
@@ -189,6 +204,7 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
   ctx->scratch.release();
   ctx->io.release();
   ctx->single.release();
+  ctx->wsbuf.release();
   delete ctx;
 }
 
@@ -212,6 +228,7 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   if (!radius && !(r_all > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
   DeviceGuard g(ctx->device);
   cudaError_t err = ensure_scratch(ctx, n_events);
+  if (err == cudaSuccess) err = ensure_ws(ctx, total);
   if (err != cudaSuccess) return cuda_error(ctx, err, "scratch allocation");
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   BatchArgs A{};
@@ -307,6 +324,8 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
     return err == cudaSuccess ? FJG_OK : cuda_error(ctx, err, "fjg_cluster_event");
   }
   if (n > fjg::kSmemMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the per-event path's particle limit");
+  cudaError_t werr = ensure_ws(ctx, n);
+  if (werr != cudaSuccess) return cuda_error(ctx, werr, "workspace allocation");
   BatchArgs A{};
   A.p4 = p4;
   A.p4_stride = 4;
@@ -349,6 +368,7 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t b_jets = al(sizeof(double) * 4 * size), b_lab = al(sizeof(int32_t) * size);
   cudaError_t err = ctx->single.reserve(b_jets + b_lab + 256);
+  if (err == cudaSuccess) err = ensure_ws(ctx, size);
   if (err != cudaSuccess) return cuda_error(ctx, err, "device buffers");
   char* d = static_cast<char*>(ctx->single.ptr);
   double* jets = reinterpret_cast<double*>(d);

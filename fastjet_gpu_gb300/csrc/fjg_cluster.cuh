@@ -1,26 +1,39 @@
-// Shared-memory-resident clustering of one event per CTA (sm_103a).
+// Clustering of one event per CTA (sm_103a), decision state in shared memory.
 //
-// Each CTA runs a persistent loop over a list of events; one event's whole
-// state lives in shared memory as a structure of arrays over "slots":
-//   FP64  rap, phi, w, nnd (dR2 to the nearest neighbour), key, px, py, pz, E
-//   FP32  rap32, phi32 (filter copies), thr (nnd rounded up)
-//   int32 nn (slot of the nearest neighbour), label (lowest constituent index)
+// Each CTA runs a persistent loop over a list of events.  Per slot (pseudojet):
+//   shared memory (what every step reads; 45 bytes a slot, so several CTAs
+//   share an SM and hide each other's serial latency):
+//     FP32  rap32, phi32                  filter coordinates
+//     FP32  wlo/whi, nlo/nhi, klo/khi     intervals bracketing the exact FP64
+//                                         weight, dR2 to the nearest neighbour,
+//                                         and key
+//     int32 nn (slot of the nearest neighbour), label (lowest constituent index)
+//     int8  pair (the key is the pair distance, not the beam distance)
+//   global workspace (L2-resident; read at merges and on the rare exact path):
+//     FP64  rap, phi, w, px, py, pz, E    exact values
 // Active pseudojets occupy slots [0, n); removing a slot moves the last active
-// slot into the hole, so scans shrink with n.  Thread t owns slots t, t+T, ...
+// slot into the hole, so scans shrink with n.
 //
-// One clustering step (reference: tri_matrix.cu:316-328 runs it as two kernel
-// launches over the full triangular matrix; n_array.cu:135-199 rescans all
-// pairs):
-//   1. argmin over (key, label): per-thread, warp redux, one barrier;
-//   2. thread 0 promotes the winner or merges it with its neighbour (E-scheme,
-//      tri_matrix.cu:247-254), recomputes kinematics, records history and
-//      compacts; one barrier;
-//   3. every thread checks its slots against the new jet (FP32 filter, exact
-//      FP64 only for candidates), collects slots whose neighbour was merged and
-//      accumulates the new jet's own neighbour search; one barrier;
-//   4. the owner warp of the new jet certifies its neighbour; slots whose
-//      neighbour disappeared are rescanned block-wide (one barrier per chunk of
-//      targets).
+// Lazy exactness.  GB300 runs FP64 at ~1/64 of the FP32 rate and charges a
+// full warp slot per FP64 instruction, so decisions are taken on FP32
+// intervals that provably contain the exact FP64 values; FP64 is evaluated
+// only when two intervals overlap (near-ties) and for the winner's recorded
+// distance.  The selection is the oracle's: argmin over (exact key, label).
+//
+// One clustering step (the reference launches two kernels per step over the
+// full triangular matrix, tri_matrix.cu:316-328):
+//   S1  argmin over (klo, label) with a certificate (klo of every other slot
+//       above the winner's khi); otherwise an exact argmin among the
+//       contenders.  One barrier (three on the rare exact path).
+//   S2  the merge warps promote the winner, or merge it with its neighbour
+//       (E-scheme, tri_matrix.cu:247-254): with two merge warps one computes
+//       the azimuth and the history record, the other the rapidity and weight
+//       and the compaction.  Meanwhile the other warps find the slots whose
+//       neighbour was the winner or its partner and scan all slots for them
+//       (named barrier), leaving per-warp certificates.  Barrier.
+//   S3  every thread checks its slots against the new jet; the owners of the
+//       rescanned slots finish their searches (adding the new jet as a
+//       candidate); barrier; the new jet's owner warp finishes its search.
 #pragma once
 
 #include "fjg_device.cuh"
@@ -31,6 +44,9 @@ struct StepRec {
   int32_t a, b;
   double d;
 };
+
+// Exact per-slot fields of the global workspace.
+enum WsField { kRap = 0, kPhi, kW, kPx, kPy, kPz, kE, kWsFields };
 
 // Description of a batch, passed by value to the kernels.
 struct BatchArgs {
@@ -44,6 +60,8 @@ struct BatchArgs {
   const int32_t* order;    // events for this kernel, in processing order
   const int32_t* n_order;  // device count of entries in order
   int* queue;              // device work counter (zeroed before launch)
+  double* ws;              // workspace: field f of slot s of event e at ws[f * ws_stride + offsets[e] + s]
+  int64_t ws_stride;       // >= total particles
   double* jets;            // [total][4]
   int32_t* jet_label;      // [total]
   int32_t* n_jets;         // [n_events]
@@ -52,42 +70,126 @@ struct BatchArgs {
   int* status;             // device error flag (0 = ok)
 };
 
-constexpr int kRescanChunk = 8;
-constexpr int kMaxWarps = 32;
+constexpr int kRescanChunk = 8;  // targets per register pass
+constexpr int kMaxTargets = 32;  // targets per step scanned during the merge
 
 template <int T, int SPT>
 struct SmemLayout {
   static constexpr int C = T * SPT;
   static constexpr int W = T / 32;
-  double rap[C], phi[C], w[C], nnd[C], key[C], px[C], py[C], pz[C], E[C];
-  float rap32[C], phi32[C], thr[C];
-  int32_t nn[C], label[C];
-  // control and reduction scratch
-  Arg warg[W];
+  float rap32[C], phi32[C], wlo[C], whi[C], nlo[C], nhi[C], klo[C], khi[C];
+  int32_t nn[C], label[C], rlist[C];
+  int8_t pair[C];
+  // reduction and control scratch
+  Cert warg[W];
+  int wlab[W], wnn[W], wpair[W];  // label, neighbour and kind of each warp's candidate
+  Arg wexact[W];
   Cert wcert[W];
-  Cert rcert[kRescanChunk][W];
-  int rlist[C];
+  Cert rcert[kMaxTargets][W];
   int n_rescan;
   int event;
-  int ctl_a, ctl_b, ctl_L, ctl_pair, ctl_njets;
+  int ctl_njets;
   double rap_max_w[W];
 };
 
-// Exact nearest neighbour of slot t among [0, n) \ {t}, from a warp-combined
-// certificate; all 32 lanes of the calling warp must call.  Returns the slot
-// (or -1) and its FP64 dR2.
+// Exact FP64 slot data of one event in the global workspace.
+struct Ws {
+  double* base;
+  int64_t stride;
+  __device__ __forceinline__ double& at(int f, int s) const { return base[f * stride + s]; }
+};
+
+// Interval of the key of a slot with weight interval [wlo, whi], neighbour
+// weight interval [vlo, vhi] and neighbour distance interval [dlo, dhi];
+// 1/R^2 interval [ilo, ihi].  Returns 1 = pair, 0 = beam, -1 = undecided (the
+// FP64 evaluation decides).  The products are rounded outwards and widened by
+// 2^-22 relative to cover the two FP64 roundings of the exact key
+// (tri_matrix.cu:112 evaluates (min(w_i, w_j) * dR2) * one_over_r2).
+__device__ __forceinline__ int key_interval(float wlo, float whi, float vlo, float vhi, float dlo, float dhi,
+                                            float ilo, float ihi, float& klo, float& khi) {
+  const float mlo = fminf(wlo, vlo), mhi = fminf(whi, vhi);
+  const float plo = __fmul_rd(__fmul_rd(__fmul_rd(mlo, dlo), ilo), 0.99999976158142089844f);
+  const float phi_ = __fmul_ru(__fmul_ru(__fmul_ru(mhi, dhi), ihi), 1.00000023841857910156f);
+  if (phi_ < wlo) {
+    klo = plo;
+    khi = phi_;
+    return 1;
+  }
+  if (plo >= whi) {
+    klo = wlo;
+    khi = whi;
+    return 0;
+  }
+  return -1;
+}
+
+struct EventCtx {
+  int N, algo;
+  double inv_r2;
+  float ilo, ihi;
+  Bound bd;
+  Ws g;
+};
+
+__device__ __forceinline__ double dr2_slots(const Ws& g, int s, int t) {
+  return dr2_64(g.at(kRap, s), g.at(kPhi, s), g.at(kRap, t), g.at(kPhi, t));
+}
+
+// Set the key of slot t from its neighbour (or none) and the neighbour
+// distance interval already stored; FP64 only when the intervals cannot decide
+// between the pair and the beam distance.
 template <int T, int SPT>
-__device__ __forceinline__ int resolve_nn_warp(SmemLayout<T, SPT>& S, int t, int n, const Cert& c, const Bound& bd,
-                                               double& d_out) {
+__device__ __forceinline__ void set_key(SmemLayout<T, SPT>& S, const EventCtx& X, int t) {
+  const int nn = S.nn[t];
+  if (nn < 0) {
+    S.klo[t] = S.wlo[t];
+    S.khi[t] = S.whi[t];
+    S.pair[t] = 0;
+    return;
+  }
+  float klo, khi;
+  const int kind = key_interval(S.wlo[t], S.whi[t], S.wlo[nn], S.whi[nn], S.nlo[t], S.nhi[t], X.ilo, X.ihi, klo, khi);
+  if (kind >= 0) {
+    S.klo[t] = klo;
+    S.khi[t] = khi;
+    S.pair[t] = (int8_t)kind;
+    return;
+  }
+  const double wt = X.g.at(kW, t);
+  const double dp = pair_distance(wt, X.g.at(kW, nn), dr2_slots(X.g, t, nn), X.inv_r2);
+  const bool is_pair = dp < wt;
+  const double key = is_pair ? dp : wt;
+  S.pair[t] = is_pair ? 1 : 0;
+  S.klo[t] = fjk_to_f32(key, 1);
+  S.khi[t] = fjk_to_f32(key, 2);
+}
+
+// The exact key of slot t (FP64), for tie resolution.  A beam key whose
+// interval is a single float is that float (e.g. C/A, where every w is 1).
+template <int T, int SPT>
+__device__ __forceinline__ double exact_key(SmemLayout<T, SPT>& S, const EventCtx& X, int t) {
+  if (!S.pair[t]) return S.klo[t] == S.khi[t] ? (double)S.klo[t] : X.g.at(kW, t);
+  const int nn = S.nn[t];
+  return pair_distance(X.g.at(kW, t), X.g.at(kW, nn), dr2_slots(X.g, t, nn), X.inv_r2);
+}
+
+// Resolve the nearest neighbour of slot t among [0, n) \ {t} from a combined
+// certificate: returns the slot (or -1) and the dR2 interval.  All 32 lanes of
+// the calling warp call.  When the certificate fails (near-tie), every
+// candidate whose lower bound does not exceed the best upper bound is
+// evaluated in FP64 and the exact minimum (dR2, label) wins.
+template <int T, int SPT>
+__device__ __forceinline__ int resolve_nn(SmemLayout<T, SPT>& S, const EventCtx& X, int t, int n, const Cert& c,
+                                          float& lo_out, float& hi_out) {
   if (c.i1 < 0) {
-    d_out = __longlong_as_double(0x7ff0000000000000LL);
+    lo_out = hi_out = __int_as_float(0x7f800000);
     return -1;
   }
   if (cert_ok(c)) {
-    d_out = dr2_64(S.rap[t], S.phi[t], S.rap[c.i1], S.phi[c.i1]);
+    lo_out = c.m1;
+    hi_out = c.u1;
     return c.i1;
   }
-  // near-tie: every slot whose lower bound does not exceed the best upper bound
   const int lane = threadIdx.x & 31;
   unsigned long long bk = ~0ull;
   int bl = 0x7fffffff, bi = -1;
@@ -95,10 +197,9 @@ __device__ __forceinline__ int resolve_nn_warp(SmemLayout<T, SPT>& S, int t, int
   for (int u = lane; u < n; u += 32) {
     if (u == t) continue;
     float lo, hi;
-    dr2_32(rt, pt, S.rap32[u], S.phi32[u], bd, lo, hi);
+    dr2_32(rt, pt, S.rap32[u], S.phi32[u], X.bd, lo, hi);
     if (lo <= c.u1) {
-      const double d = dr2_64(S.rap[t], S.phi[t], S.rap[u], S.phi[u]);
-      const unsigned long long k = dbits(d);
+      const unsigned long long k = dbits(dr2_slots(X.g, t, u));
       if (arg_less(k, S.label[u], bk, bl)) {
         bk = k;
         bl = S.label[u];
@@ -107,19 +208,114 @@ __device__ __forceinline__ int resolve_nn_warp(SmemLayout<T, SPT>& S, int t, int
     }
   }
   const Arg r = arg_warp(bk, bl, bi);
-  d_out = __longlong_as_double((long long)r.key);
+  const double d = __longlong_as_double((long long)r.key);
+  lo_out = fjk_to_f32(d, 1);
+  hi_out = fjk_to_f32(d, 2);
   return r.idx;
+}
+
+// Whole-warp nearest-neighbour search for slot t over [0, n) \ {t}.
+template <int T, int SPT>
+__device__ __forceinline__ int warp_nn_search(SmemLayout<T, SPT>& S, const EventCtx& X, int t, int n, float& lo,
+                                              float& hi) {
+  Cert c = cert_empty();
+  const float rt = S.rap32[t], pt = S.phi32[t];
+  for (int u = threadIdx.x & 31; u < n; u += 32) {
+    if (u == t) continue;
+    float l, h;
+    dr2_32(rt, pt, S.rap32[u], S.phi32[u], X.bd, l, h);
+    cert_add(c, l, h, u);
+  }
+  c = cert_warp(c);
+  return resolve_nn<T, SPT>(S, X, t, n, c, lo, hi);
+}
+
+// One pass of the rescan warps over the final slots for up to K targets
+// (rlist[base .. base+cnt)): per-warp certificates into rcert.  Final slot u's
+// data sits in slot u, except u == b whose data is still in slot L; slot a (the
+// new jet, being written) is skipped.
+template <int K, int T, int SPT>
+__device__ __forceinline__ void rescan_chunk(SmemLayout<T, SPT>& S, const EventCtx& X, int base, int cnt, int r0,
+                                             int TR, int n_new, int a, int b, int L) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  Cert rc[K];
+  int tgt[K];
+  float rt[K], pt[K];
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    rc[r] = cert_empty();
+    tgt[r] = (r < cnt) ? S.rlist[base + r] : -1;
+    const int sr = (r < cnt) ? (tgt[r] == b ? L : tgt[r]) : 0;
+    rt[r] = S.rap32[sr];
+    pt[r] = S.phi32[sr];
+  }
+  for (int u = r0; u < n_new; u += TR) {
+    if (u == a) continue;
+    const int su = u == b ? L : u;
+    const float ru = S.rap32[su], pu = S.phi32[su];
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+      if (r < cnt && u != tgt[r]) {
+        float lo, hi;
+        dr2_32(rt[r], pt[r], ru, pu, X.bd, lo, hi);
+        cert_add(rc[r], lo, hi, u);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    if (r < cnt) {
+      const Cert wc = cert_warp(rc[r]);
+      if (lane == 0) S.rcert[base + r][warp] = wc;
+    }
+  }
+}
+
+// Named barriers: 1 among the rescan warps, 2 among the merge warps.
+__device__ __forceinline__ void named_sync(int id, int threads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// Move slot `from` into slot `to` (shared state by lane 0, workspace fields by
+// lanes 1..7 of the calling warp; every lane calls).
+template <int T, int SPT>
+__device__ __forceinline__ void move_slot_warp(SmemLayout<T, SPT>& S, const Ws& g, int to, int from) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    S.rap32[to] = S.rap32[from];
+    S.phi32[to] = S.phi32[from];
+    S.wlo[to] = S.wlo[from];
+    S.whi[to] = S.whi[from];
+    S.nlo[to] = S.nlo[from];
+    S.nhi[to] = S.nhi[from];
+    S.klo[to] = S.klo[from];
+    S.khi[to] = S.khi[from];
+    S.nn[to] = S.nn[from];
+    S.label[to] = S.label[from];
+    S.pair[to] = S.pair[from];
+  } else if (lane <= kWsFields) {
+    g.at(lane - 1, to) = g.at(lane - 1, from);
+  }
 }
 
 template <int T, int SPT>
 __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, int e) {
   constexpr int W = T / 32;
+  constexpr int MW = (T >= 128) ? 3 : 1;  // merge warps
+  constexpr int TR = T - 32 * MW;         // rescan threads
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t off = A.offsets[e];
-  const int N = (int)(A.offsets[e + 1] - off);
-  const int algo = A.algo ? A.algo[e] : A.algo_all;
+  EventCtx X;
+  X.N = (int)(A.offsets[e + 1] - off);
+  X.algo = A.algo ? A.algo[e] : A.algo_all;
   const double R = A.radius ? A.radius[e] : A.r_all;
-  const double inv_r2 = 1.0 / (R * R);
+  X.inv_r2 = 1.0 / (R * R);
+  X.ilo = fjk_to_f32(X.inv_r2, 1);
+  X.ihi = fjk_to_f32(X.inv_r2, 2);
+  X.g.base = A.ws + off;
+  X.g.stride = A.ws_stride;
+  const Ws& g = X.g;
+  const int N = X.N;
 
   // ---- load and kinematics
   double rmax = 0.0;
@@ -128,26 +324,32 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
     if (s >= N) break;
     const double* p = A.p4 + (off + s) * A.p4_stride;
     const double px = p[0], py = p[1], pz = p[2], E = p[3];
-    const Kin kin = kinematics(px, py, pz, E, algo);
-    S.px[s] = px;
-    S.py[s] = py;
-    S.pz[s] = pz;
-    S.E[s] = E;
-    S.rap[s] = kin.rap;
-    S.phi[s] = kin.phi;
-    S.w[s] = kin.w;
-    S.rap32[s] = __double2float_rn(kin.rap);
-    S.phi32[s] = __double2float_rn(kin.phi);
+    const Kin kin = kinematics(px, py, pz, E, X.algo);
+    g.at(kPx, s) = px;
+    g.at(kPy, s) = py;
+    g.at(kPz, s) = pz;
+    g.at(kE, s) = E;
+    g.at(kRap, s) = kin.rap;
+    g.at(kPhi, s) = kin.phi;
+    g.at(kW, s) = kin.w;
+    S.rap32[s] = fjk_to_f32(kin.rap, 0);
+    S.phi32[s] = fjk_to_f32(kin.phi, 0);
+    S.wlo[s] = fjk_to_f32(kin.w, 1);
+    S.whi[s] = fjk_to_f32(kin.w, 2);
     S.label[s] = s;
     rmax = fmax(rmax, fabs(kin.rap));
     if (A.owner) A.owner[off + s] = s;  // union-find parent by label
   }
   for (int o = 16; o; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(kFull, rmax, o));
   if (lane == 0) S.rap_max_w[warp] = rmax;
+  if (tid == 0) {
+    S.ctl_njets = 0;
+    S.n_rescan = 0;
+  }
   __syncthreads();
   rmax = 0.0;
   for (int k = 0; k < W; ++k) rmax = fmax(rmax, S.rap_max_w[k]);
-  const Bound bd = make_bound(rmax);
+  X.bd = make_bound(rmax);
 
   // ---- initial nearest neighbours (each slot scans all others)
   for (int k = 0; k < SPT; ++k) {
@@ -158,151 +360,287 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
     for (int u = 0; u < N; ++u) {
       if (u == t) continue;
       float lo, hi;
-      dr2_32(rt, pt, S.rap32[u], S.phi32[u], bd, lo, hi);
+      dr2_32(rt, pt, S.rap32[u], S.phi32[u], X.bd, lo, hi);
       cert_add(c, lo, hi, u);
     }
     int nn = c.i1;
-    double d = __longlong_as_double(0x7ff0000000000000LL);
-    if (nn >= 0) {
-      if (cert_ok(c)) {
-        d = dr2_64(S.rap[t], S.phi[t], S.rap[nn], S.phi[nn]);
-      } else {
-        unsigned long long bk = ~0ull;
-        int bl = 0x7fffffff;
-        nn = -1;
-        for (int u = 0; u < N; ++u) {
-          if (u == t) continue;
-          float lo, hi;
-          dr2_32(rt, pt, S.rap32[u], S.phi32[u], bd, lo, hi);
-          if (lo <= c.u1) {
-            const double du = dr2_64(S.rap[t], S.phi[t], S.rap[u], S.phi[u]);
-            if (arg_less(dbits(du), S.label[u], bk, bl)) {
-              bk = dbits(du);
-              bl = S.label[u];
-              nn = u;
-            }
+    float nlo = c.m1, nhi = c.u1;
+    if (nn >= 0 && !cert_ok(c)) {
+      unsigned long long bk = ~0ull;
+      int bl = 0x7fffffff;
+      nn = -1;
+      for (int u = 0; u < N; ++u) {
+        if (u == t) continue;
+        float lo, hi;
+        dr2_32(rt, pt, S.rap32[u], S.phi32[u], X.bd, lo, hi);
+        if (lo <= c.u1) {
+          const unsigned long long du = dbits(dr2_slots(g, t, u));
+          if (arg_less(du, S.label[u], bk, bl)) {
+            bk = du;
+            bl = S.label[u];
+            nn = u;
           }
         }
-        d = __longlong_as_double((long long)bk);
       }
+      const double d = __longlong_as_double((long long)bk);
+      nlo = fjk_to_f32(d, 1);
+      nhi = fjk_to_f32(d, 2);
     }
     S.nn[t] = nn;
-    S.nnd[t] = d;
-    S.thr[t] = __double2float_ru(d);
+    S.nlo[t] = nlo;
+    S.nhi[t] = nhi;
   }
   __syncthreads();
   for (int k = 0; k < SPT; ++k) {
     const int t = tid + k * T;
     if (t >= N) break;
-    const int nn = S.nn[t];
-    S.key[t] = make_key(S.w[t], nn >= 0 ? S.w[nn] : 0.0, S.nnd[t], inv_r2, nn >= 0);
+    set_key<T, SPT>(S, X, t);
   }
-  if (tid == 0) S.ctl_njets = 0;
   __syncthreads();
 
   // ---- clustering steps
   int n = N;
   int step = 0;
   while (n > 0) {
-    // 1. argmin over (key, label)
-    unsigned long long bk = ~0ull;
-    int bl = 0x7fffffff, bi = -1;
+    // S1: argmin over (klo, label) with a certificate.  The winner's neighbour
+    // and kind travel with the reduction: once B1 is passed the merge warps
+    // may overwrite the winner's slot (compaction) while other warps are still
+    // deciding what to do.
+    Cert mine = cert_empty();
+    int mlab = 0x7fffffff, mnn = -1, mpair = 0;
     for (int k = 0; k < SPT; ++k) {
       const int t = tid + k * T;
       if (t >= n) break;
-      const unsigned long long kk = dbits(S.key[t]);
+      const float lo = S.klo[t];
       const int l = S.label[t];
-      if (arg_less(kk, l, bk, bl)) {
-        bk = kk;
-        bl = l;
-        bi = t;
+      if (lo < mine.m1 || (lo == mine.m1 && l < mlab)) {
+        mine.m2 = mine.m1;
+        mine.m1 = lo;
+        mine.u1 = S.khi[t];
+        mine.i1 = t;
+        mlab = l;
+        mnn = S.nn[t];
+        mpair = S.pair[t];
+      } else {
+        mine.m2 = fminf(mine.m2, lo);
       }
     }
-    Arg wa = arg_warp(bk, bl, bi);
-    if (lane == 0) S.warg[warp] = wa;
+    {
+      // warp combine: smallest klo, then lowest label
+      const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(mine.m1));
+      const bool at_min = __float_as_uint(mine.m1) == mb && mine.i1 >= 0;
+      const unsigned lb = __reduce_min_sync(kFull, at_min ? (unsigned)mlab : 0xffffffffu);
+      const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)mlab == lb);
+      const int src = ball ? __ffs(ball) - 1 : 0;
+      Cert wc;
+      wc.m1 = __uint_as_float(mb);
+      wc.i1 = __shfl_sync(kFull, mine.i1, src);
+      wc.u1 = __shfl_sync(kFull, mine.u1, src);
+      if (!ball) wc.i1 = -1;
+      const unsigned other = (ball && lane == src) ? __float_as_uint(mine.m2) : __float_as_uint(mine.m1);
+      wc.m2 = __uint_as_float(__reduce_min_sync(kFull, other));
+      const int wnn = __shfl_sync(kFull, mnn, src);
+      const int wpair = __shfl_sync(kFull, mpair, src);
+      if (lane == 0) {
+        S.warg[warp] = wc;
+        S.wlab[warp] = ball ? (int)lb : 0x7fffffff;
+        S.wnn[warp] = wnn;
+        S.wpair[warp] = wpair;
+      }
+    }
     __syncthreads();  // B1
-    if (tid < 32) {
-      Arg x = (lane < W) ? S.warg[lane] : Arg{~0ull, 0x7fffffff, -1};
-      x = arg_warp(x.key, x.label, x.idx);
-      // 2. promote or merge (thread 0)
-      if (tid == 0 && x.idx < 0) {
-        // no candidate although n > 0: cannot happen for finite inputs; stop this event
-        atomicOr(A.status, 4);
-        S.ctl_pair = -1;
-      } else if (tid == 0) {
-        const int s = x.idx;
-        const double key = S.key[s];
-        const int L = n - 1;
-        int a = -1, b;
-        int pair = 0;
-        if (key < S.w[s] && S.nn[s] >= 0) {
-          pair = 1;
-          const int j = S.nn[s];
-          a = min(s, j);
-          b = max(s, j);
-          const int la = S.label[s], lb = S.label[j];
-          const int lo_l = min(la, lb), hi_l = max(la, lb);
-          const double px = __dadd_rn(S.px[s], S.px[j]);
-          const double py = __dadd_rn(S.py[s], S.py[j]);
-          const double pz = __dadd_rn(S.pz[s], S.pz[j]);
-          const double E = __dadd_rn(S.E[s], S.E[j]);
-          const Kin kin = kinematics(px, py, pz, E, algo);
-          S.px[a] = px;
-          S.py[a] = py;
-          S.pz[a] = pz;
-          S.E[a] = E;
-          S.rap[a] = kin.rap;
-          S.phi[a] = kin.phi;
-          S.w[a] = kin.w;
-          S.rap32[a] = __double2float_rn(kin.rap);
-          S.phi32[a] = __double2float_rn(kin.phi);
+    int c, cnn, cpair;
+    float u1;
+    bool certified;
+    {
+      const Cert x = (lane < W) ? S.warg[lane] : cert_empty();
+      const int xl = (lane < W) ? S.wlab[lane] : 0x7fffffff;
+      const int xnn = (lane < W) ? S.wnn[lane] : -1;
+      const int xpair = (lane < W) ? S.wpair[lane] : 0;
+      const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(x.m1));
+      const bool at_min = __float_as_uint(x.m1) == mb && x.i1 >= 0;
+      const unsigned lb = __reduce_min_sync(kFull, at_min ? (unsigned)xl : 0xffffffffu);
+      const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)xl == lb);
+      const int src = ball ? __ffs(ball) - 1 : 0;
+      c = __shfl_sync(kFull, x.i1, src);
+      if (!ball) c = -1;
+      u1 = __shfl_sync(kFull, x.u1, src);
+      cnn = __shfl_sync(kFull, xnn, src);
+      cpair = __shfl_sync(kFull, xpair, src);
+      const unsigned other = (ball && lane == src) ? __float_as_uint(x.m2) : __float_as_uint(x.m1);
+      const float m2 = __uint_as_float(__reduce_min_sync(kFull, other));
+      certified = (c >= 0) && (u1 < m2);
+    }
+    if (!certified && c >= 0) {
+      // near-tie (every thread takes this branch: same shared inputs): exact
+      // keys of all slots whose klo does not exceed the winner's khi
+      __syncthreads();  // everyone has read warg
+      unsigned long long bk = ~0ull;
+      int bl = 0x7fffffff, bi = -1, bnn = -1, bpair = 0;
+      for (int k = 0; k < SPT; ++k) {
+        const int t = tid + k * T;
+        if (t >= n) break;
+        if (S.klo[t] <= u1) {
+          const unsigned long long kk = dbits(exact_key<T, SPT>(S, X, t));
+          if (arg_less(kk, S.label[t], bk, bl)) {
+            bk = kk;
+            bl = S.label[t];
+            bi = t;
+            bnn = S.nn[t];
+            bpair = S.pair[t];
+          }
+        }
+      }
+      const Arg wa = arg_warp(bk, bl, bi);
+      const unsigned wball = __ballot_sync(kFull, bi == wa.idx && bi >= 0);
+      const int wsrc = wball ? __ffs(wball) - 1 : 0;
+      const int wnn = __shfl_sync(kFull, bnn, wsrc);
+      const int wpair = __shfl_sync(kFull, bpair, wsrc);
+      if (lane == 0) {
+        S.wexact[warp] = wa;
+        S.wnn[warp] = wnn;
+        S.wpair[warp] = wpair;
+      }
+      __syncthreads();
+      const Arg y = (lane < W) ? S.wexact[lane] : Arg{~0ull, 0x7fffffff, -1};
+      const int ynn = (lane < W) ? S.wnn[lane] : -1;
+      const int ypair = (lane < W) ? S.wpair[lane] : 0;
+      const Arg win = arg_warp(y.key, y.label, y.idx);
+      const unsigned yball = __ballot_sync(kFull, y.idx == win.idx && y.idx >= 0);
+      const int ysrc = yball ? __ffs(yball) - 1 : 0;
+      c = win.idx;
+      cnn = __shfl_sync(kFull, ynn, ysrc);
+      cpair = __shfl_sync(kFull, ypair, ysrc);
+      __syncthreads();  // wexact, wnn, wpair may be reused in the next step
+    }
+    if (c < 0) {  // no candidate although n > 0: cannot happen for finite inputs
+      if (tid == 0) atomicOr(A.status, 4);
+      break;
+    }
+
+    // S2: decisions every thread takes from the same values
+    const bool pair = cpair != 0 && cnn >= 0;
+    const int j = pair ? cnn : -1;
+    const int a = pair ? min(c, j) : -1;
+    const int b = pair ? max(c, j) : c;
+    const int L = n - 1;
+    const int n_new = n - 1;
+
+    if (warp < MW) {
+      // Merge warps.  With three: warp 0 computes the azimuth, warp 1 the
+      // rapidity and four-momentum, warp 2 the weight and the history record
+      // and then compacts (its chain is the shortest); with one, warp 0 does
+      // all of it.  Everything read
+      // of slots c and j is read before barrier 2 (or before the compaction):
+      // the compaction may overwrite one of those slots.
+      const int role = (MW == 1) ? -1 : warp;
+      double pxc = 0, pyc = 0, pzc = 0, Ec = 0, pxj = 0, pyj = 0, pzj = 0, Ej = 0;
+      double rc = 0, fc = 0, wc = 0, rj = 0, fj = 0, wj = 0;
+      int lc = 0, lj = 0;
+      if (lane == 0) {
+        pxc = g.at(kPx, c);
+        pyc = g.at(kPy, c);
+        pzc = g.at(kPz, c);
+        Ec = g.at(kE, c);
+        wc = g.at(kW, c);
+        lc = S.label[c];
+        if (pair) {
+          pxj = g.at(kPx, j);
+          pyj = g.at(kPy, j);
+          pzj = g.at(kPz, j);
+          Ej = g.at(kE, j);
+          wj = g.at(kW, j);
+          lj = S.label[j];
+          rc = g.at(kRap, c);
+          fc = g.at(kPhi, c);
+          rj = g.at(kRap, j);
+          fj = g.at(kPhi, j);
+        }
+      }
+      __syncwarp();
+      if (MW > 1) named_sync(2, 32 * MW);  // every merge warp holds its inputs
+      const int lo_l = pair ? min(lc, lj) : lc, hi_l = max(lc, lj);
+      const bool phi_role = role <= 0, rap_role = role == -1 || role == 1, w_role = role == -1 || role == 2;
+      if (pair) {
+        const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
+        if (lane == 0 && phi_role) {
+          const double phi = fjk_phi(px, py);
+          g.at(kPhi, a) = phi;
+          S.phi32[a] = fjk_to_f32(phi, 0);
+        }
+        if (lane == 0 && rap_role) {
+          const double pz = __dadd_rn(pzc, pzj), E = __dadd_rn(Ec, Ej);
+          const double rap = fjk_rap(px, py, pz, E);
+          g.at(kPx, a) = px;
+          g.at(kPy, a) = py;
+          g.at(kPz, a) = pz;
+          g.at(kE, a) = E;
+          g.at(kRap, a) = rap;
+          S.rap32[a] = fjk_to_f32(rap, 0);
           S.label[a] = lo_l;
-          if (A.history) A.history[off + step] = StepRec{lo_l, hi_l, key};
+        }
+        if (lane == 0 && w_role) {
+          const double w = fjk_weight(px, py, X.algo);
+          g.at(kW, a) = w;
+          S.wlo[a] = fjk_to_f32(w, 1);
+          S.whi[a] = fjk_to_f32(w, 2);
+          const double d = pair_distance(wc, wj, dr2_64(rc, fc, rj, fj), X.inv_r2);
+          if (A.history) A.history[off + step] = StepRec{lo_l, hi_l, d};
           if (A.owner) A.owner[off + hi_l] = lo_l;
-        } else {
-          b = s;
-          const int nj = S.ctl_njets;
-          double* jo = A.jets + (off + nj) * 4;
-          jo[0] = S.px[s];
-          jo[1] = S.py[s];
-          jo[2] = S.pz[s];
-          jo[3] = S.E[s];
-          A.jet_label[off + nj] = S.label[s];
-          if (A.history) A.history[off + step] = StepRec{S.label[s], -1, key};
-          if (A.owner) A.owner[off + S.label[s]] = -(nj + 1);
-          S.ctl_njets = nj + 1;
         }
-        if (b != L) {
-          S.rap[b] = S.rap[L];
-          S.phi[b] = S.phi[L];
-          S.w[b] = S.w[L];
-          S.nnd[b] = S.nnd[L];
-          S.key[b] = S.key[L];
-          S.px[b] = S.px[L];
-          S.py[b] = S.py[L];
-          S.pz[b] = S.pz[L];
-          S.E[b] = S.E[L];
-          S.rap32[b] = S.rap32[L];
-          S.phi32[b] = S.phi32[L];
-          S.thr[b] = S.thr[L];
-          S.nn[b] = S.nn[L];
-          S.label[b] = S.label[L];
+      } else if (lane == 0 && w_role) {
+        const int nj = S.ctl_njets;
+        double* jo = A.jets + (off + nj) * 4;
+        jo[0] = pxc;
+        jo[1] = pyc;
+        jo[2] = pzc;
+        jo[3] = Ec;
+        A.jet_label[off + nj] = lc;
+        if (A.history) A.history[off + step] = StepRec{lc, -1, wc};
+        if (A.owner) A.owner[off + lc] = -(nj + 1);
+        S.ctl_njets = nj + 1;
+      }
+      if (w_role) {
+        __syncwarp();
+        if (b != L) move_slot_warp<T, SPT>(S, g, b, L);  // compaction (never touches slot a)
+      }
+      __syncwarp();
+    } else {
+      // Rescan targets: final slots (slot L moves to b) whose neighbour was c or
+      // j.  While the merge warps write slots a and b, these warps read
+      // neither: data of final slot u is read from src(u) (= L for u == b), and
+      // a is skipped.
+      const int r0 = tid - 32 * MW;
+      for (int u = r0; u < n_new; u += TR) {
+        if (u == a) continue;
+        const int nu = S.nn[u == b ? L : u];
+        if (nu == c || (pair && nu == j)) {
+          const int pos = atomicAdd(&S.n_rescan, 1);
+          S.rlist[pos] = u;
         }
-        S.ctl_a = a;
-        S.ctl_b = b;
-        S.ctl_L = L;
-        S.ctl_pair = pair;
-        S.n_rescan = 0;
+      }
+      named_sync(1, TR);
+      const int nr = min(S.n_rescan, kMaxTargets);
+      for (int base = 0; base < nr; base += kRescanChunk) {
+        const int cnt = min(kRescanChunk, nr - base);
+        if (cnt == 1)
+          rescan_chunk<1, T, SPT>(S, X, base, cnt, r0, TR, n_new, a, b, L);
+        else if (cnt == 2)
+          rescan_chunk<2, T, SPT>(S, X, base, cnt, r0, TR, n_new, a, b, L);
+        else if (cnt <= 4)
+          rescan_chunk<4, T, SPT>(S, X, base, cnt, r0, TR, n_new, a, b, L);
+        else
+          rescan_chunk<8, T, SPT>(S, X, base, cnt, r0, TR, n_new, a, b, L);
       }
     }
-    __syncthreads();  // B2
-    if (S.ctl_pair < 0) break;
-    --n;
+    __syncthreads();  // B2: new jet and compaction written, rescan partials ready
+    n = n_new;
     ++step;
-    const int a = S.ctl_a, b = S.ctl_b, L = S.ctl_L;
-    const bool pair = S.ctl_pair != 0;
+    if (n == 0) break;
+    const int nr_all = S.n_rescan;
+    const int nr = min(nr_all, kMaxTargets);
 
-    // 3. update against the new jet; collect rescans
+    // S3: every slot against the new jet; finish the rescans
     Cert ca = cert_empty();
     float ra = 0.f, pa = 0.f;
     if (pair) {
@@ -312,106 +650,95 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
     for (int k = 0; k < SPT; ++k) {
       const int t = tid + k * T;
       if (t >= n) break;
-      if (pair && t == a) continue;
-      int c = S.nn[t];
-      const bool resc = pair ? (c == a || c == b) : (c == b);
-      if (!resc && c == L) {
-        c = b;
+      if (t == a) continue;
+      int cn = S.nn[t];  // still in the numbering before this step
+      const bool target = (cn == c || (pair && cn == j));
+      float lo = 0.f, hi = 0.f;
+      if (pair) {
+        dr2_32(S.rap32[t], S.phi32[t], ra, pa, X.bd, lo, hi);
+        cert_add(ca, lo, hi, t);
+      }
+      if (target) continue;
+      if (cn == L) {
+        cn = b;
         S.nn[t] = b;
       }
-      if (resc) {
-        const int pos = atomicAdd(&S.n_rescan, 1);
-        S.rlist[pos] = t;
+      if (!pair) continue;
+      const float nlo = S.nlo[t], nhi = S.nhi[t];
+      bool closer;
+      float ulo = lo, uhi = hi;
+      if (hi < nlo) {
+        closer = true;
+      } else if (lo > nhi) {
+        closer = false;
+      } else {
+        const double da = dr2_slots(g, t, a);
+        const double dc = dr2_slots(g, t, cn);
+        closer = da < dc || (da == dc && S.label[a] < S.label[cn]);
+        ulo = fjk_to_f32(da, 1);
+        uhi = fjk_to_f32(da, 2);
       }
-      if (pair) {
-        float lo, hi;
-        dr2_32(S.rap32[t], S.phi32[t], ra, pa, bd, lo, hi);
-        cert_add(ca, lo, hi, t);
-        if (!resc && lo <= S.thr[t]) {
-          const double d = dr2_64(S.rap[t], S.phi[t], S.rap[a], S.phi[a]);
-          const double D = S.nnd[t];
-          if (d < D || (d == D && S.label[a] < S.label[c])) {
-            S.nn[t] = a;
-            S.nnd[t] = d;
-            S.thr[t] = __double2float_ru(d);
-            S.key[t] = make_key(S.w[t], S.w[a], d, inv_r2, true);
-          }
-        }
+      if (closer) {
+        S.nn[t] = a;
+        S.nlo[t] = ulo;
+        S.nhi[t] = uhi;
+        set_key<T, SPT>(S, X, t);
       }
     }
     if (pair) {
       const Cert wc = cert_warp(ca);
       if (lane == 0) S.wcert[warp] = wc;
     }
-    __syncthreads();  // B3
-
-    // 4a. the new jet's neighbour: owner warp combines and certifies
+    // finish the scanned targets: the owner warp combines the rescan warps'
+    // partials with the new jet
+    for (int r = 0; r < nr; ++r) {
+      const int t = S.rlist[r];
+      if (warp != (t % T) / 32) continue;
+      Cert x = (lane >= MW && lane < W) ? S.rcert[r][lane] : cert_empty();
+      if (pair && lane == 0) {
+        float lo, hi;
+        dr2_32(S.rap32[t], S.phi32[t], ra, pa, X.bd, lo, hi);
+        cert_add(x, lo, hi, a);
+      }
+      x = cert_warp(x);
+      float lo, hi;
+      const int nn = resolve_nn<T, SPT>(S, X, t, n, x, lo, hi);
+      if (tid == t % T) {
+        S.nn[t] = nn;
+        S.nlo[t] = lo;
+        S.nhi[t] = hi;
+        set_key<T, SPT>(S, X, t);
+      }
+    }
+    // targets beyond one S2 pass (a slot is the neighbour of many others only
+    // in degenerate inputs such as repeated particles): one warp each
+    for (int r = kMaxTargets + warp; r < nr_all; r += W) {
+      const int t = S.rlist[r];
+      float lo, hi;
+      const int nn = warp_nn_search<T, SPT>(S, X, t, n, lo, hi);
+      if (lane == 0) {
+        S.nn[t] = nn;
+        S.nlo[t] = lo;
+        S.nhi[t] = hi;
+        set_key<T, SPT>(S, X, t);
+      }
+      __syncwarp();
+    }
+    __syncthreads();  // B3: the new jet's partials are ready
     if (pair && warp == (a % T) / 32) {
-      Cert c = (lane < W) ? S.wcert[lane] : cert_empty();
-      c = cert_warp(c);
-      double d;
-      const int nn = resolve_nn_warp<T, SPT>(S, a, n, c, bd, d);
+      Cert x = (lane < W) ? S.wcert[lane] : cert_empty();
+      x = cert_warp(x);
+      float lo, hi;
+      const int nn = resolve_nn<T, SPT>(S, X, a, n, x, lo, hi);
       if (tid == a % T) {
         S.nn[a] = nn;
-        S.nnd[a] = d;
-        S.thr[a] = __double2float_ru(d);
-        S.key[a] = make_key(S.w[a], nn >= 0 ? S.w[nn] : 0.0, d, inv_r2, nn >= 0);
+        S.nlo[a] = lo;
+        S.nhi[a] = hi;
+        set_key<T, SPT>(S, X, a);
       }
     }
-
-    // 4b. rescans of slots whose neighbour was merged or promoted
-    const int nr = S.n_rescan;
-    for (int base = 0; base < nr; base += kRescanChunk) {
-      const int cnt = min(kRescanChunk, nr - base);
-      Cert rc[kRescanChunk];
-      int tgt[kRescanChunk];
-      float rt[kRescanChunk], pt[kRescanChunk];
-#pragma unroll
-      for (int r = 0; r < kRescanChunk; ++r) {
-        rc[r] = cert_empty();
-        tgt[r] = (r < cnt) ? S.rlist[base + r] : -1;
-        rt[r] = (r < cnt) ? S.rap32[tgt[r]] : 0.f;
-        pt[r] = (r < cnt) ? S.phi32[tgt[r]] : 0.f;
-      }
-      for (int k = 0; k < SPT; ++k) {
-        const int u = tid + k * T;
-        if (u >= n) break;
-        const float ru = S.rap32[u], pu = S.phi32[u];
-#pragma unroll
-        for (int r = 0; r < kRescanChunk; ++r) {
-          if (r < cnt && u != tgt[r]) {
-            float lo, hi;
-            dr2_32(rt[r], pt[r], ru, pu, bd, lo, hi);
-            cert_add(rc[r], lo, hi, u);
-          }
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < kRescanChunk; ++r) {
-        if (r < cnt) {
-          const Cert wc = cert_warp(rc[r]);
-          if (lane == 0) S.rcert[r][warp] = wc;
-        }
-      }
-      __syncthreads();  // B4
-      for (int r = 0; r < cnt; ++r) {
-        const int t = tgt[r];
-        if (warp != (t % T) / 32) continue;
-        Cert c = (lane < W) ? S.rcert[r][lane] : cert_empty();
-        c = cert_warp(c);
-        double d;
-        const int nn = resolve_nn_warp<T, SPT>(S, t, n, c, bd, d);
-        if (tid == t % T) {
-          S.nn[t] = nn;
-          S.nnd[t] = d;
-          S.thr[t] = __double2float_ru(d);
-          S.key[t] = make_key(S.w[t], nn >= 0 ? S.w[nn] : 0.0, d, inv_r2, nn >= 0);
-        }
-      }
-      if (base + kRescanChunk < nr) __syncthreads();  // rcert reuse
-    }
-    // the next argmin reads only keys its own thread wrote, or keys written
-    // before B2/B3/B4 by other threads
+    if (tid == 0) S.n_rescan = 0;
+    // the next S1 reads keys written by their owner thread, or before B3
   }
 
   // ---- epilogue: jet count, and constituent ownership from the union-find

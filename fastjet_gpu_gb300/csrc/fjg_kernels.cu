@@ -20,29 +20,89 @@ __global__ void __launch_bounds__(T) k_cluster_smem(BatchArgs A) {
   }
 }
 
-// Distribute events into size buckets; empty events are finished here.
-__global__ void k_bucket(const int64_t* offsets, int n_events, int32_t* order, int32_t* counts, int cap_events,
-                         int32_t* n_jets, int* status) {
+// Events are handed to the bucket kernels largest first (longest-processing-
+// time order), so that the biggest events do not start last and form the tail.
+// Three passes: a size histogram, a descending scan that also yields each
+// bucket's count, and a scatter into per-bucket lists.  Empty events are
+// finished in the first pass; oversize ones raise the status word.
+
+__global__ void k_size_hist(const int64_t* offsets, int n_events, int32_t* hist, int32_t* n_jets, int* status) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
     const int64_t n64 = offsets[e + 1] - offsets[e];
-    if (n64 < 0) {
-      atomicOr(status, kStatusBadArg);
+    if (n64 <= 0 || n64 > kSmemMaxN) {
       n_jets[e] = 0;
+      if (n64 < 0) atomicOr(status, kStatusBadArg);
+      if (n64 > kSmemMaxN) atomicOr(status, kStatusTooBig);
       continue;
     }
-    if (n64 == 0) {
-      n_jets[e] = 0;
-      continue;
-    }
-    const int b = (n64 > kSmemMaxN) ? -1 : bucket_of((int)n64);
-    if (b < 0) {
-      atomicOr(status, kStatusTooBig);
-      n_jets[e] = 0;
-      continue;
-    }
-    const int pos = atomicAdd(&counts[b], 1);
-    order[b * cap_events + pos] = e;
+    atomicAdd(&hist[n64], 1);
   }
+}
+
+// One block of 1024 threads: hist[n] becomes the position of the first event
+// of size n inside its bucket's list (sizes in descending order), counts[b]
+// the number of events of bucket b.
+__global__ void __launch_bounds__(1024) k_size_scan(int32_t* hist, int32_t* counts) {
+  __shared__ int32_t warp_sum[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // thread tid owns sizes n = kSmemMaxN - 2 tid and kSmemMaxN - 2 tid - 1 (descending)
+  const int n0 = kSmemMaxN - 2 * tid, n1 = n0 - 1;
+  const int h0 = hist[n0], h1 = (n1 >= 1) ? hist[n1] : 0;
+  int incl = h0 + h1;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_sum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int v = warp_sum[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    warp_sum[lane] = v;
+  }
+  __syncthreads();
+  const int before = incl - h0 - h1 + (warp > 0 ? warp_sum[warp - 1] : 0);  // events larger than n0
+  // the start of a bucket in the descending order is the number of larger events
+  const int b0 = bucket_of(n0);
+  __shared__ int32_t bucket_start[kNumBuckets + 1];
+  // sizes 256 << b are the largest of bucket b: their "before" is the bucket start
+  for (int b = 0; b < kNumBuckets; ++b)
+    if (n0 == (256 << b)) bucket_start[b] = before;
+    else if (n1 == (256 << b)) bucket_start[b] = before + h0;
+  if (tid == 0) bucket_start[kNumBuckets] = 0;
+  __syncthreads();
+  const int total = warp_sum[31];
+  hist[n0] = before - bucket_start[b0];
+  if (n1 >= 1) hist[n1] = before + h0 - bucket_start[bucket_of(n1)];
+  if (tid < kNumBuckets) {
+    // bucket b spans positions [start_b, start_{b-1}) of the descending order
+    const int hi = bucket_start[tid];
+    const int lo_next = (tid == 0) ? total : bucket_start[tid - 1];
+    counts[tid] = lo_next - hi;
+  }
+}
+
+__global__ void k_size_scatter(const int64_t* offsets, int n_events, int32_t* hist, int32_t* order, int cap_events) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
+    const int64_t n64 = offsets[e + 1] - offsets[e];
+    if (n64 <= 0 || n64 > kSmemMaxN) continue;
+    const int pos = atomicAdd(&hist[n64], 1);
+    order[bucket_of((int)n64) * cap_events + pos] = e;
+  }
+}
+
+static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_events, cudaStream_t stream) {
+  cudaError_t err;
+  if ((err = cudaMemsetAsync(sc.hist, 0, sizeof(int32_t) * kHistBins, stream)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumBuckets, stream)) != cudaSuccess) return err;
+  const int grid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
+  k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status);
+  k_size_scan<<<1, 1024, 0, stream>>>(sc.hist, sc.counts);
+  k_size_scatter<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, sc.order, sc.cap_events);
+  return cudaGetLastError();
 }
 
 template <int T, int SPT>
@@ -74,9 +134,9 @@ static int blocks_per_sm() {
 static cudaError_t launch_bucket_dispatch(int b, const BatchArgs& A, int grid, cudaStream_t s) {
   switch (b) {
     case 0: return launch_bucket<64, 4>(A, grid, s);
-    case 1: return launch_bucket<128, 4>(A, grid, s);
-    case 2: return launch_bucket<256, 4>(A, grid, s);
-    default: return launch_bucket<512, 4>(A, grid, s);
+    case 1: return launch_bucket<64, 8>(A, grid, s);
+    case 2: return launch_bucket<128, 8>(A, grid, s);
+    default: return launch_bucket<256, 8>(A, grid, s);
   }
 }
 
@@ -85,9 +145,9 @@ static int bucket_blocks_per_sm(int b) {
   if (cache[b] == 0) {
     switch (b) {
       case 0: cache[b] = blocks_per_sm<64, 4>(); break;
-      case 1: cache[b] = blocks_per_sm<128, 4>(); break;
-      case 2: cache[b] = blocks_per_sm<256, 4>(); break;
-      default: cache[b] = blocks_per_sm<512, 4>(); break;
+      case 1: cache[b] = blocks_per_sm<64, 8>(); break;
+      case 2: cache[b] = blocks_per_sm<128, 8>(); break;
+      default: cache[b] = blocks_per_sm<256, 8>(); break;
     }
   }
   return cache[b];
@@ -95,13 +155,8 @@ static int bucket_blocks_per_sm(int b) {
 
 cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
                          cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join) {
-  cudaError_t err;
-  if ((err = cudaMemsetAsync(sc.counts, 0, sizeof(int32_t) * kNumBuckets, stream)) != cudaSuccess) return err;
-  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumBuckets, stream)) != cudaSuccess) return err;
-  const int bgrid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
-  k_bucket<<<bgrid, 256, 0, stream>>>(base.offsets, n_events, sc.order, sc.counts, sc.cap_events, base.n_jets,
-                                      sc.status);
-  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  cudaError_t err = launch_sort(base, sc, n_events, stream);
+  if (err != cudaSuccess) return err;
   if ((err = cudaEventRecord(*ev_fork, stream)) != cudaSuccess) return err;
   // largest events first: their bucket is launched first
   for (int b = kNumBuckets - 1; b >= 0; --b) {
@@ -111,6 +166,8 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
     A.order = sc.order + b * sc.cap_events;
     A.n_order = sc.counts + b;
     A.queue = sc.queues + b;
+    A.ws = sc.ws;
+    A.ws_stride = sc.ws_stride;
     int grid = num_sms * bucket_blocks_per_sm(b);
     if (grid > n_events) grid = n_events;
     if (grid < 1) grid = 1;
@@ -125,18 +182,15 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
 
 cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
                                    cudaStream_t stream) {
-  cudaError_t err;
-  if ((err = cudaMemsetAsync(sc.counts, 0, sizeof(int32_t) * kNumBuckets, stream)) != cudaSuccess) return err;
-  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumBuckets, stream)) != cudaSuccess) return err;
-  const int bgrid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
-  k_bucket<<<bgrid, 256, 0, stream>>>(base.offsets, n_events, sc.order, sc.counts, sc.cap_events, base.n_jets,
-                                      sc.status);
-  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  cudaError_t err = launch_sort(base, sc, n_events, stream);
+  if (err != cudaSuccess) return err;
   for (int b = kNumBuckets - 1; b >= 0; --b) {
     BatchArgs A = base;
     A.order = sc.order + b * sc.cap_events;
     A.n_order = sc.counts + b;
     A.queue = sc.queues + b;
+    A.ws = sc.ws;
+    A.ws_stride = sc.ws_stride;
     int grid = num_sms * bucket_blocks_per_sm(b);
     if (grid > n_events) grid = n_events;
     if (grid < 1) grid = 1;
@@ -166,6 +220,8 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaS
   A.order = sc.order;
   A.n_order = sc.counts;
   A.queue = sc.queues;
+  A.ws = sc.ws;
+  A.ws_stride = sc.ws_stride;
   return launch_bucket_dispatch(b, A, 1, stream);
 }
 

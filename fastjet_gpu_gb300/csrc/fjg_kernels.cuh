@@ -7,11 +7,13 @@
 
 namespace fjg {
 
-// Size buckets of the shared-memory path: capacity C = threads * 4 slots.
+// Size buckets of the shared-memory path: bucket b holds events of up to
+// 256 << b particles, run by CTAs of 64, 64, 128, 256 threads (4, 8, 8, 8
+// slots per thread): 45 bytes of shared memory per slot and ~120 registers
+// per thread let 8, 8, 4 and 2 CTAs share an SM.
 constexpr int kNumBuckets = 4;
 constexpr int kSmemMaxN = 2048;
 
-// bucket b holds events of up to 256 << b particles, run by CTAs of 64 << b threads
 __host__ __device__ inline int bucket_of(int n) {
   return n <= 256 ? 0 : n <= 512 ? 1 : n <= 1024 ? 2 : n <= 2048 ? 3 : -1;
 }
@@ -19,7 +21,7 @@ __host__ __device__ inline int bucket_of(int n) {
 // Status bits raised by kernels (ORed into the device status word).
 enum : int { kStatusTooBig = 1, kStatusBadArg = 2, kStatusInternal = 4 };
 
-static_assert(sizeof(SmemLayout<512, 4>) <= 232448, "bucket 3 exceeds the opt-in shared memory per block");
+static_assert(sizeof(SmemLayout<256, 8>) <= 232448 / 2, "bucket 3: two CTAs per SM");
 
 // Device-side batch descriptor scratch owned by a context.
 struct Scratch {
@@ -29,7 +31,12 @@ struct Scratch {
   int* status;      // [1]
   int64_t* offsets1;  // [2] single-event offsets {0, n}
   int cap_events;
+  double* ws;         // [kWsFields][ws_stride] exact per-particle state
+  int64_t ws_stride;  // particles the workspace holds
+  int32_t* hist;      // [kHistBins] events per size, then per-size positions (sorting by size)
 };
+
+constexpr int kHistBins = kSmemMaxN + 1;
 
 // Launch the bucketing kernel plus one persistent kernel per bucket on
 // `stream` (buckets run concurrently on the side streams when given).

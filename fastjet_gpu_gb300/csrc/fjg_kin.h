@@ -15,12 +15,13 @@
 //                     scale 2^-112; one final rounding.  Positive normal x only
 //                     (else FJK_LIBM_LOG).  Absolute error ~2^-75, relative
 //                     precision kept near x = 1;
-//   fjk_atan2(y, x)   octant reduction to t = min/max in [0, 1] (quotient to
-//                     128 bits); for t >= 2^-6 the table atan(k/256) plus
-//                     atan(d), d = (t - c)/(1 + t c), |d| <= 2^-9, odd series
-//                     to d^7, at scale 2^-120; for t < 2^-5 the series
-//                     t (1 - t^2/3 + ... - t^12/13) with relative precision;
-//                     one final rounding.  Finite nonzero normal operands only
+//   fjk_atan2(y, x)   octant reduction to t = min/max in [0, 1]; for t >= 2^-6
+//                     the table atan(c), c = k/256 nearest to t, plus atan(d),
+//                     d = (t - c)/(1 + t c) = (num - c den)/(den + c num) as
+//                     one exact integer division, |d| <= 2^-9, odd series to
+//                     d^7, at scale 2^-120; for t < 2^-5 the series
+//                     t (1 - t^2/3 + ... - t^12/13) on a 128-bit quotient,
+//                     with relative precision; one final rounding.  Finite nonzero normal operands only
 //                     (else FJK_LIBM_ATAN2).
 // The results are the correctly rounded values except when the exact value
 // lies within ~2^-12 ulp of a rounding boundary; the tests measure the
@@ -100,18 +101,79 @@ FJK_FN uint64_t fjk_mulhi_u(uint64_t a, uint64_t b) { return (uint64_t)(((fjk_u1
 
 FJK_FN int64_t fjk_mulhi_s(int64_t a, int64_t b) { return (int64_t)(((fjk_i128)a * b) >> 64); }
 
-// V ~ floor(2^127 / D) for D in [2^63, 2^64); never above the true value, at
-// most a few units below.  FP32 reciprocal seed (24 bits) and two Newton steps.
-FJK_FN uint64_t fjk_recip64(uint64_t D) {
-  const float df = (float)(uint32_t)(D >> 40);  // in [2^23, 2^24), exact
+FJK_FN float fjk_float_of(uint32_t b) {
 #if defined(__CUDACC__)
-  const float rf = __frcp_rn(df);
+  return __uint_as_float(b);
 #else
-  const float rf = 1.0f / df;
+  union {
+    float f;
+    uint32_t u;
+  } c;
+  c.u = b;
+  return c.f;
 #endif
-  uint64_t V = (uint64_t)(rf * 77371252455336267181195264.0f);  // rf * 2^86, in (2^62, 2^63]
-  V -= V >> 21;                                                   // make it an underestimate
-  V <<= 1;
+}
+
+FJK_FN uint32_t fjk_bits_of(float f) {
+#if defined(__CUDACC__)
+  return __float_as_uint(f);
+#else
+  union {
+    float f;
+    uint32_t u;
+  } c;
+  c.f = f;
+  return c.u;
+#endif
+}
+
+// double -> float with round-to-nearest-even (mode 0), toward -inf (mode 1)
+// or toward +inf (mode 2), from the bit pattern (the hardware conversion is a
+// ~90-cycle operation on GB300).  Results outside the float normal range and
+// non-finite inputs use the hardware conversion.
+FJK_FN float fjk_to_f32(double x, int mode) {
+  const uint64_t b = fjk_bits(x);
+  const uint32_t sign = (uint32_t)(b >> 63);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+  if (e < 1 || e > 254) {
+#if defined(__CUDACC__)
+    return mode == 0 ? __double2float_rn(x) : mode == 1 ? __double2float_rd(x) : __double2float_ru(x);
+#else
+    // host: round to nearest, then step outward if that went the wrong way
+    float f = (float)x;
+    if (mode == 1 && (double)f > x) f = nextafterf(f, -INFINITY);
+    if (mode == 2 && (double)f < x) f = nextafterf(f, INFINITY);
+    return f;
+#endif
+  }
+  const uint64_t m = b & FJK_MASK52;
+  const uint32_t rem = (uint32_t)(m & 0x1fffffffu);  // the 29 bits below the float mantissa
+  const uint32_t out = (sign << 31) | ((uint32_t)e << 23) | (uint32_t)(m >> 29);
+  int up;
+  if (mode == 0)
+    up = rem > 0x10000000u || (rem == 0x10000000u && (out & 1));
+  else if (mode == 1)
+    up = sign && rem;  // the magnitude grows toward -inf for negatives
+  else
+    up = !sign && rem;
+  return fjk_float_of(out + (uint32_t)up);  // a carry moves into the exponent (or to inf)
+}
+
+// V ~ floor(2^127 / D) for D in [2^63, 2^64); never above the true value, at
+// most a few units below.  The FP32 reciprocal of the top 24 bits of D seeds
+// two Newton steps in 64-bit fixed point.  The seed is built from and read
+// back into bit patterns: integer<->float conversions cost ~90 cycles on
+// GB300, the bit moves a few.
+FJK_FN uint64_t fjk_recip64(uint64_t D) {
+  const float f = fjk_float_of(0x3f800000u | ((uint32_t)(D >> 40) & 0x7fffffu));  // top bits, in [1, 2)
+#if defined(__CUDACC__)
+  const float r = __frcp_rn(f);
+#else
+  const float r = 1.0f / f;
+#endif
+  const uint32_t rb = fjk_bits_of(r);  // r in (1/2, 1]
+  uint64_t V = ((rb >> 23) < 127u) ? ((uint64_t)((rb & 0x7fffffu) | 0x800000u) << 40) : ~0ull;  // r 2^64
+  V -= V >> 21;  // make it an underestimate
   for (int it = 0; it < 2; ++it) {
     const fjk_u128 e = ((fjk_u128)1 << 127) - (fjk_u128)D * V;  // > 0
     V += (uint64_t)(((fjk_u128)V * (uint64_t)(e >> 64)) >> 63);
@@ -242,19 +304,19 @@ FJK_FN double fjk_atan2(double y, double x) {
   if (exn == 0 || eyn == 0 || exn == 0x7ff || eyn == 0x7ff) return FJK_LIBM_ATAN2(y, x);
   const int swap = ay > ax;  // |y| > |x|
   const uint64_t nb = swap ? ax : ay, db = swap ? ay : ax;
-  const int k = (int)(db >> 52) - (int)(nb >> 52);  // >= 0
+  const int k = (int)(db >> 52) - (int)(nb >> 52);  // >= 0; t = (Mn / Md) 2^-k <= 1
   if (k > 1000) return FJK_LIBM_ATAN2(y, x);          // result near the subnormal range
   const uint64_t Mn = (nb & FJK_MASK52) | FJK_HID52, Md = (db & FJK_MASK52) | FJK_HID52;
-  const uint64_t D = Md << 11;
-  const uint64_t V = fjk_recip64(D);
-  uint64_t r1, r2;
-  const uint64_t Q1 = fjk_divq((fjk_u128)Mn << 74, D, V, &r1);  // (Mn/Md) 2^63
-  const uint64_t Q2 = fjk_divq((fjk_u128)r1 << 64, D, V, &r2);  // next 64 bits
-  const fjk_u128 Tq = ((fjk_u128)Q1 << 64) | Q2;                // t = Tq 2^-(127+k)
   const int x_neg = (int)(xb >> 63), y_neg = (int)(yb >> 63);
   fjk_i128 res;  // atan(t) at scale 2^-120
   if (k >= 6) {
-    // t < 2^-5: atan(t) = t (1 - corr), corr = t^2/3 - t^4/5 + ... - t^12/13
+    // t < 2^-5: t to 128 bits, atan(t) = t (1 - corr), corr = t^2/3 - ... - t^12/13
+    const uint64_t D = Md << 11;
+    const uint64_t V = fjk_recip64(D);
+    uint64_t r1, r2;
+    const uint64_t Q1 = fjk_divq((fjk_u128)Mn << 74, D, V, &r1);  // (Mn/Md) 2^63
+    const uint64_t Q2 = fjk_divq((fjk_u128)r1 << 64, D, V, &r2);  // next 64 bits
+    const fjk_u128 Tq = ((fjk_u128)Q1 << 64) | Q2;                // t = Tq 2^-(127+k)
     const int sh = 2 * k - 2;  // t^2 at scale 2^-64 = (Q1^2 >> 64) >> (2k - 2)
     const uint64_t t2 = sh >= 64 ? 0 : (fjk_mulhi_u(Q1, Q1) >> sh);
     uint64_t p = FJK_AQ13;
@@ -269,25 +331,35 @@ FJK_FN double fjk_atan2(double y, double x) {
     if (!swap && !x_neg) return fjk_round_fixed(At, 127 + k, y_neg);
     res = (fjk_i128)(At >> (7 + k));
   } else {
-    const fjk_u128 t120 = Tq >> (7 + k);                       // t <= 1 at scale 2^-120
-    const int kk = (int)((t120 + ((fjk_u128)1 << 111)) >> 112);  // round(256 t)
-    const fjk_i128 u = (fjk_i128)t120 - ((fjk_i128)kk << 112);   // t - c, |.| <= 2^-9
+    // nearest table point c = kk/256 from an FP32 estimate of t (bit patterns)
+    const float fn = fjk_float_of(0x3f800000u | (uint32_t)((Mn >> 29) & 0x7fffffu));
+    const float fd = fjk_float_of(0x3f800000u | (uint32_t)((Md >> 29) & 0x7fffffu));
+    const uint32_t tb = fjk_bits_of(fn / fd);         // Mn/Md in (1/2, 2)
+    const int et = (int)(tb >> 23) - 127;             // -1 or 0
+    const uint32_t mt = (tb & 0x7fffffu) | 0x800000u;  // 24-bit mantissa
+    const int s = 15 - et + k;                         // 256 t = mt 2^-s
+    int kk = (int)((mt + (1u << (s - 1))) >> s);
+    kk = kk > 256 ? 256 : kk;
+    // d = (t - c) / (1 + t c) = N / Dd exactly, with both scaled by 256 Md 2^k
+    const fjk_i128 N = ((fjk_i128)Mn << 8) - ((fjk_i128)((fjk_u128)Md * (uint64_t)kk) << k);
+    const fjk_u128 Dd = ((fjk_u128)Md << (8 + k)) + (fjk_u128)Mn * (uint64_t)kk;  // in [2^60, 2^67)
     res = fjk_i128_of(FJK_ATAN_HI[kk], FJK_ATAN_LO[kk]);
-    if (u != 0) {
-      const fjk_u128 v = ((fjk_u128)1 << 120) + (t120 >> 8) * (fjk_u128)kk;  // 1 + t c < 2
-      const uint64_t Dv = (uint64_t)(v >> 57);                               // [2^63, 2^64)
-      const uint64_t Vv = fjk_recip64(Dv);
-      const fjk_u128 au = (fjk_u128)(u < 0 ? -u : u);
+    if (N != 0) {
+      const uint64_t dh = (uint64_t)(Dd >> 64);
+      const int bl = dh ? 128 - fjk_clz64(dh) : 64 - fjk_clz64((uint64_t)Dd);  // bit length, 61..67
+      const int sh = bl - 64;                                                 // -4..3
+      const uint64_t Dn = (uint64_t)(sh >= 0 ? (Dd >> sh) : (Dd << -sh));    // [2^63, 2^64)
+      const fjk_u128 aN = (fjk_u128)(N < 0 ? -N : N);
       uint64_t rr;
-      const uint64_t d72 = fjk_divq(au << 15, Dv, Vv, &rr);  // |d| at scale 2^-72, <= 2^63
-      const uint64_t d2 = fjk_mulhi_u(d72, d72);            // d^2 at scale 2^-80
+      const uint64_t d72 = fjk_divq(aN << (72 - sh), Dn, fjk_recip64(Dn), &rr);  // |d| 2^72, < 2^63
+      const uint64_t d2 = fjk_mulhi_u(d72, d72);                                  // d^2 at scale 2^-80
       uint64_t p = FJK_AQ7;
       p = FJK_AQ5 - (fjk_mulhi_u(d2, p) >> 16);
       p = FJK_AQ3 - (fjk_mulhi_u(d2, p) >> 16);
       const uint64_t corr = fjk_mulhi_u(d2, p) >> 16;      // d^2 P at scale 2^-64
       const uint64_t ad72 = d72 - fjk_mulhi_u(d72, corr);  // atan(|d|) at scale 2^-72
       const fjk_i128 add = (fjk_i128)((fjk_u128)ad72 << 48);
-      res = (u < 0) ? res - add : res + add;
+      res = (N < 0) ? res - add : res + add;
     }
   }
   if (swap) res = fjk_i128_of(FJK_PI_2_120_HI, FJK_PI_2_120_LO) - res;
@@ -297,26 +369,47 @@ FJK_FN double fjk_atan2(double y, double x) {
 
 // The reference's pseudojet kinematics (tri_matrix.cu:61-100, weights
 // grid.cu:153-166) with fjk_atan2 / fjk_log / fjk_div_rn in place of the libm
-// calls and divisions; every other operation rounds as written.
-FJK_FN void fjk_kinematics(double px, double py, double pz, double E, int algo, double* rap_out, double* phi_out,
-                           double* w_out) {
+// calls and divisions; every other operation rounds as written.  Split in two
+// so that the azimuth and the rapidity/weight chains can run on different
+// warps.
+
+// Azimuth in [0, 2pi).
+FJK_FN double fjk_phi(double px, double py) {
   const double kTwoPi = 6.283185307179586476925286766559005768394;
   const double pt2 = FJK_DADD(FJK_DMUL(px, px), FJK_DMUL(py, py));
   double phi = (pt2 == 0.0) ? 0.0 : fjk_atan2(py, px);
   if (phi < 0.0) phi = FJK_DADD(phi, kTwoPi);
   if (phi >= kTwoPi) phi = FJK_DSUB(phi, kTwoPi);
+  return phi;
+}
+
+// Rapidity (MaxRap = 1e5 branch for E == |pz|, pt == 0).
+FJK_FN double fjk_rap(double px, double py, double pz, double E) {
+  const double pt2 = FJK_DADD(FJK_DMUL(px, px), FJK_DMUL(py, py));
   const double apz = fabs(pz);
-  double rap;
   if (E == apz && pt2 == 0.0) {
     const double mr = FJK_DADD(1e5, apz);
-    rap = (pz >= 0.0) ? mr : -mr;
-  } else {
-    const double m2 = fmax(0.0, FJK_DSUB(FJK_DMUL(FJK_DADD(E, pz), FJK_DSUB(E, pz)), pt2));
-    const double epz = FJK_DADD(E, apz);
-    rap = fjk_log_scaled(fjk_div_rn(FJK_DADD(pt2, m2), FJK_DMUL(epz, epz)), 1);
-    if (pz > 0.0) rap = -rap;
+    return (pz >= 0.0) ? mr : -mr;
   }
-  *rap_out = rap;
-  *phi_out = phi;
-  *w_out = (algo == 1) ? pt2 : (algo == 0) ? 1.0 : ((pt2 > 1e-300) ? fjk_div_rn(1.0, pt2) : 1e300);
+  const double m2 = fmax(0.0, FJK_DSUB(FJK_DMUL(FJK_DADD(E, pz), FJK_DSUB(E, pz)), pt2));
+  const double epz = FJK_DADD(E, apz);
+  const double rap = fjk_log_scaled(fjk_div_rn(FJK_DADD(pt2, m2), FJK_DMUL(epz, epz)), 1);
+  return (pz > 0.0) ? -rap : rap;
+}
+
+// Clustering weight: kt pt^2, C/A 1, anti-kt 1/pt^2 (1e300 below pt^2 = 1e-300).
+FJK_FN double fjk_weight(double px, double py, int algo) {
+  const double pt2 = FJK_DADD(FJK_DMUL(px, px), FJK_DMUL(py, py));
+  return (algo == 1) ? pt2 : (algo == 0) ? 1.0 : ((pt2 > 1e-300) ? fjk_div_rn(1.0, pt2) : 1e300);
+}
+
+FJK_FN void fjk_rap_w(double px, double py, double pz, double E, int algo, double* rap_out, double* w_out) {
+  *rap_out = fjk_rap(px, py, pz, E);
+  *w_out = fjk_weight(px, py, algo);
+}
+
+FJK_FN void fjk_kinematics(double px, double py, double pz, double E, int algo, double* rap_out, double* phi_out,
+                           double* w_out) {
+  *phi_out = fjk_phi(px, py);
+  fjk_rap_w(px, py, pz, E, algo, rap_out, w_out);
 }

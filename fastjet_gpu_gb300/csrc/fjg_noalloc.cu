@@ -28,9 +28,12 @@
 namespace {
 
 constexpr int kNoAllocMaxEvents = FJG_NOALLOC_MAX_EVENTS;
+constexpr int kNoAllocMaxParticles = FJG_NOALLOC_MAX_PARTICLES;
 
 struct NoAllocScratch {
+  double ws[fjg::kWsFields * kNoAllocMaxParticles];    // exact per-particle state (overwritten per event)
   int32_t order[fjg::kNumBuckets * kNoAllocMaxEvents];  // per-bucket event lists
+  int32_t hist[fjg::kHistBins];                        // size histogram (zeroed per call)
   int32_t counts[fjg::kNumBuckets];                    // events per bucket (zeroed per call)
   int32_t queues[fjg::kNumBuckets];                    // work-queue heads (zeroed per call)
   int32_t status;                                      // kernel error bits (zeroed per call)
@@ -52,13 +55,16 @@ fjg_status fail(fjg_status st, const char* msg) {
 }  // namespace
 
 extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t* offsets, int n_events,
-                                                const int32_t* algo, int algo_all, const double* radius,
-                                                double r_all, const fjg_outputs* out, void* stream) {
+                                                int64_t total, const int32_t* algo, int algo_all,
+                                                const double* radius, double r_all, const fjg_outputs* out,
+                                                void* stream) {
   if (n_events < 0 || !offsets || !out || !out->n_jets) return fail(FJG_EINVAL, "bad batch arguments");
   if (n_events > kNoAllocMaxEvents)
     return fail(FJG_EINVAL, "fjg_cluster_batch_noalloc: more events than FJG_NOALLOC_MAX_EVENTS in one call");
   if (n_events == 0) return FJG_OK;
   if (!p4 || !out->jets || !out->jet_label) return fail(FJG_EINVAL, "null buffer");
+  if (total < 0 || total > kNoAllocMaxParticles)
+    return fail(FJG_EINVAL, "fjg_cluster_batch_noalloc: more particles than FJG_NOALLOC_MAX_PARTICLES in one call");
   if (!algo && !(algo_all == FJG_KT || algo_all == FJG_CAM || algo_all == FJG_ANTIKT))
     return fail(FJG_EINVAL, "bad algorithm");
   if (!radius && !(r_all > 0.0)) return fail(FJG_EINVAL, "R must be positive");
@@ -92,6 +98,9 @@ extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t*
   sc.status = &sc_dev->status;
   sc.offsets1 = nullptr;
   sc.cap_events = kNoAllocMaxEvents;
+  sc.hist = sc_dev->hist;
+  sc.ws = sc_dev->ws;
+  sc.ws_stride = kNoAllocMaxParticles;
 
   fjg::BatchArgs A{};
   A.p4 = p4;

@@ -63,6 +63,8 @@ def lib():
         for f in ("fjo_kin_atan2", "fjo_kin_div"):
             getattr(L, f).argtypes = [ctypes.c_double, ctypes.c_double]
             getattr(L, f).restype = ctypes.c_double
+        L.fjo_kin_f32.argtypes = [ctypes.c_double, ctypes.c_int]
+        L.fjo_kin_f32.restype = ctypes.c_float
         L.fjo_kin_kinematics.argtypes = [P, ctypes.c_int, P, P, P]
         L.fjo_kin_kinematics.restype = None
         _lib = L

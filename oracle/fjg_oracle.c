@@ -87,6 +87,7 @@ static inline int closer(double d, int32_t l, double bd, int32_t bl) { return d 
 double fjo_kin_log(double x) { return fjk_log(x); }
 double fjo_kin_atan2(double y, double x) { return fjk_atan2(y, x); }
 double fjo_kin_div(double a, double b) { return fjk_div_rn(a, b); }
+float fjo_kin_f32(double x, int mode) { return fjk_to_f32(x, mode); }
 void fjo_kin_kinematics(const double p4[4], int algo, double* rap, double* phi, double* w) {
   fjk_kinematics(p4[0], p4[1], p4[2], p4[3], algo, rap, phi, w);
 }

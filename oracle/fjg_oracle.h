@@ -51,6 +51,7 @@ void fjo_kinematics(const double p4[4], int algo, double* pt2, double* phi, doub
 double fjo_kin_log(double x);
 double fjo_kin_atan2(double y, double x);
 double fjo_kin_div(double a, double b);
+float fjo_kin_f32(double x, int mode); /* mode 0: nearest, 1: toward -inf, 2: toward +inf */
 void fjo_kin_kinematics(const double p4[4], int algo, double* rap, double* phi, double* w);
 
 /* Cluster one event of n particles (p4: [n][4] px,py,pz,E).

@@ -35,6 +35,45 @@ def test_division_is_correctly_rounded():
         assert L.fjo_kin_div(x, y) == x / y or not (1e-308 < x / y < 1e308)
 
 
+def test_float_conversions():
+    """fjk_to_f32: nearest matches IEEE conversion; the directed modes bracket x tightly."""
+    L = oracle.lib()
+    rng = np.random.default_rng(4)
+    xs = np.concatenate([rng.normal(size=5000) * np.exp(rng.uniform(-90, 90, 5000)),
+                         [0.0, -0.0, 1.0, -1.0, 0.1, 1e300, -1e300, 1e-300, 2.0 ** -126, 6.283185307179586]])
+    with np.errstate(over="ignore"):
+        for x in xs:
+            rn = L.fjo_kin_f32(float(x), 0)
+            assert np.float32(rn).tobytes() == np.float32(x).tobytes(), x
+            rd, ru = np.float32(L.fjo_kin_f32(float(x), 1)), np.float32(L.fjo_kin_f32(float(x), 2))
+            assert float(rd) <= x <= float(ru), x
+            if float(rd) == x:
+                assert rd == ru
+            elif np.isfinite(rd) and np.isfinite(ru):
+                assert np.nextafter(rd, np.float32(np.inf)) == ru, x
+
+
+def test_atan2_table_boundaries():
+    """t = |y/x| next to every table point k/256 and around the small-t branch."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 160
+    L = oracle.lib()
+    bad = 0
+    n = 0
+    for kk in range(0, 257, 3):
+        for eps in (0.0, 1e-12, -1e-12, 1e-6, 0.5 / 256 - 1e-9):
+            t = kk / 256 + eps
+            if not 0 < t <= 1:
+                continue
+            for y, x in ((t, 1.0), (1.0, t), (-t, -1.0), (t * 3.7, -3.7)):
+                v = L.fjo_kin_atan2(y, x)
+                c = float(mpmath.atan2(mpmath.mpf(y), mpmath.mpf(x)))
+                n += 1
+                bad += v != c
+                assert _ulps(v, c) <= 1
+    assert bad <= 0.001 * n
+
+
 def test_log_and_atan2_against_correct_rounding():
     mpmath = pytest.importorskip("mpmath")
     mpmath.mp.prec = 160

@@ -19,8 +19,8 @@ pytestmark = pytest.mark.gpu
 
 def _run_noalloc(F, torch, batch, algo, radius):
     L = F.lib()
-    L.fjg_cluster_batch_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
-                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
+    L.fjg_cluster_batch_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64,
+                                            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
                                             ctypes.POINTER(F._Outputs), ctypes.c_void_p]
     dev = torch.device("cuda", 0)
     total = int(batch.offsets[-1])
@@ -36,7 +36,7 @@ def _run_noalloc(F, torch, batch, algo, radius):
     out = F._Outputs(jets.data_ptr(), lab.data_ptr(), nj.data_ptr(), hist.data_ptr(), None)
     stream = torch.cuda.current_stream(dev).cuda_stream
     torch.cuda.synchronize()
-    st = L.fjg_cluster_batch_noalloc(ctypes.c_void_p(p4.data_ptr()), ctypes.c_void_p(off.data_ptr()), ne,
+    st = L.fjg_cluster_batch_noalloc(ctypes.c_void_p(p4.data_ptr()), ctypes.c_void_p(off.data_ptr()), ne, total,
                                      ctypes.c_void_p(a_t.data_ptr()) if a_t is not None else None,
                                      int(algo) if a_t is None else 0,
                                      ctypes.c_void_p(r_t.data_ptr()) if r_t is not None else None,
@@ -54,8 +54,9 @@ def test_noalloc_matches_batch_entry_point_twice():
     import fastjet_gpu_gb300 as F
     from fastjet_gpu_gb300 import events as E
 
-    first = E.mixed_batch(300, 20, 2048, seed=71)
-    second, algo2, radius2 = E.serving_mix(200, seed=72, lo=2, hi=2048)
+    first = E.mixed_batch(120, 20, 2048, seed=71)
+    second, algo2, radius2 = E.serving_mix(60, seed=72, lo=2, hi=2048)
+    assert first.offsets[-1] <= 131072 and second.offsets[-1] <= 131072
     ctx = F.Context(0)
     for batch, algo, radius in ((first, -1, 0.4), (second, algo2, radius2)):
         got = _run_noalloc(F, torch, batch, algo, radius)
