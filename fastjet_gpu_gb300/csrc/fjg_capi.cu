@@ -47,14 +47,15 @@ struct fjg_ctx {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t side[fjg::kNumBuckets] = {};
+  cudaStream_t side[fjg::kNumQueues] = {};
   cudaEvent_t ev_fork = nullptr;
-  cudaEvent_t ev_join[fjg::kNumBuckets] = {};
+  cudaEvent_t ev_join[fjg::kNumQueues] = {};
   fjg::Scratch sc{};
   DeviceBuffer scratch;  // order/counts/queues/status/offsets1
   DeviceBuffer io;       // device copies for the host-memory entry points
   DeviceBuffer single;   // outputs of fjg_cluster_pseudojets
   DeviceBuffer wsbuf;    // exact per-particle state of the clustering kernels
+  DeviceBuffer largebuf; // state of the tiled kernel (events above 2048 particles)
   std::string last_error;
 };
 
@@ -92,7 +93,7 @@ cudaError_t ensure_scratch(fjg_ctx* ctx, int n_events) {
   if (ctx->sc.order && ctx->sc.cap_events >= n_events) return cudaSuccess;
   int cap = n_events + n_events / 4 + 64;
   const size_t hist_bytes = (sizeof(int32_t) * fjg::kHistBins + 255) & ~size_t(255);
-  size_t bytes = sizeof(int32_t) * (size_t)fjg::kNumBuckets * cap + 256 + hist_bytes;
+  size_t bytes = sizeof(int32_t) * (size_t)fjg::kNumQueues * cap + 256 + hist_bytes;
   cudaError_t err = ctx->scratch.reserve(bytes);
   if (err != cudaSuccess) return err;
   char* p = static_cast<char*>(ctx->scratch.ptr);
@@ -117,6 +118,18 @@ cudaError_t ensure_ws(fjg_ctx* ctx, int64_t particles) {
   if (err != cudaSuccess) return err;
   ctx->sc.ws = static_cast<double*>(ctx->wsbuf.ptr);
   ctx->sc.ws_stride = (int64_t)(ctx->wsbuf.cap / (sizeof(double) * fjg::kWsFields));
+  return cudaSuccess;
+}
+
+// Ensure the tiled kernel's workspace covers `particles` entries (batches
+// whose particles all fit the shared-memory path need none).
+cudaError_t ensure_large_ws(fjg_ctx* ctx, int64_t particles) {
+  if (particles <= fjg::kSmemMaxN) return cudaSuccess;
+  if (ctx->sc.large_ws && ctx->sc.large_ws_particles >= particles) return cudaSuccess;
+  cudaError_t err = ctx->largebuf.reserve((size_t)fjg::kLargeWsBytesPerParticle * (size_t)particles + 256);
+  if (err != cudaSuccess) return err;
+  ctx->sc.large_ws = static_cast<unsigned char*>(ctx->largebuf.ptr);
+  ctx->sc.large_ws_particles = (int64_t)((ctx->largebuf.cap - 256) / fjg::kLargeWsBytesPerParticle);
   return cudaSuccess;
 }
 
@@ -173,7 +186,7 @@ fjg_status fjg_ctx_create(int device, fjg_ctx** out) {
   DeviceGuard g(device);
   err = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-  for (int b = 0; b < fjg::kNumBuckets && err == cudaSuccess; ++b) {
+  for (int b = 0; b < fjg::kNumQueues && err == cudaSuccess; ++b) {
     err = cudaStreamCreateWithFlags(&ctx->side[b], cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ctx->ev_join[b], cudaEventDisableTiming);
   }
@@ -192,7 +205,7 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
   if (!ctx) return;
   DeviceGuard g(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  for (int b = 0; b < fjg::kNumBuckets; ++b) {
+  for (int b = 0; b < fjg::kNumQueues; ++b) {
     if (ctx->side[b]) {
       cudaStreamSynchronize(ctx->side[b]);
       cudaStreamDestroy(ctx->side[b]);
@@ -205,6 +218,7 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
   ctx->io.release();
   ctx->single.release();
   ctx->wsbuf.release();
+  ctx->largebuf.release();
   delete ctx;
 }
 
@@ -213,7 +227,7 @@ void* fjg_ctx_stream(fjg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; 
 fjg_status fjg_ctx_check(fjg_ctx* ctx) {
   if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
   DeviceGuard g(ctx->device);
-  for (int b = 0; b < fjg::kNumBuckets; ++b) cudaStreamSynchronize(ctx->side[b]);
+  for (int b = 0; b < fjg::kNumQueues; ++b) cudaStreamSynchronize(ctx->side[b]);
   return take_status(ctx, ctx->stream);
 }
 
@@ -229,6 +243,7 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   DeviceGuard g(ctx->device);
   cudaError_t err = ensure_scratch(ctx, n_events);
   if (err == cudaSuccess) err = ensure_ws(ctx, total);
+  if (err == cudaSuccess) err = ensure_large_ws(ctx, total);
   if (err != cudaSuccess) return cuda_error(ctx, err, "scratch allocation");
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   BatchArgs A{};
@@ -323,8 +338,9 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
     return err == cudaSuccess ? FJG_OK : cuda_error(ctx, err, "fjg_cluster_event");
   }
-  if (n > fjg::kSmemMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the per-event path's particle limit");
+  if (n > fjg::kLargeMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the supported particle count");
   cudaError_t werr = ensure_ws(ctx, n);
+  if (werr == cudaSuccess) werr = ensure_large_ws(ctx, n);
   if (werr != cudaSuccess) return cuda_error(ctx, werr, "workspace allocation");
   BatchArgs A{};
   A.p4 = p4;
@@ -362,13 +378,14 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
   if (!valid_algo(algo)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
   if (!(r > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
   if (size == 0) return FJG_OK;
-  if (size > fjg::kSmemMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the supported particle count");
+  if (size > fjg::kLargeMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the supported particle count");
   DeviceGuard g(ctx->device);
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t b_jets = al(sizeof(double) * 4 * size), b_lab = al(sizeof(int32_t) * size);
   cudaError_t err = ctx->single.reserve(b_jets + b_lab + 256);
   if (err == cudaSuccess) err = ensure_ws(ctx, size);
+  if (err == cudaSuccess) err = ensure_large_ws(ctx, size);
   if (err != cudaSuccess) return cuda_error(ctx, err, "device buffers");
   char* d = static_cast<char*>(ctx->single.ptr);
   double* jets = reinterpret_cast<double*>(d);

@@ -68,6 +68,7 @@ struct BatchArgs {
   StepRec* history;        // [total] or null
   int32_t* owner;          // [total] or null
   int* status;             // device error flag (0 = ok)
+  unsigned char* large_ws; // tiled-path workspace: event e at large_ws + 96 * offsets[e] (null: none)
 };
 
 constexpr int kRescanChunk = 8;  // targets per register pass

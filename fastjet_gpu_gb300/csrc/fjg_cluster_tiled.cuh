@@ -1,0 +1,908 @@
+// Clustering of large events (more than 2048 particles): one CTA per event,
+// state in a global workspace, nearest neighbours restricted to a 3x3 window
+// of rapidity-azimuth tiles.  (The reference's grid backend, grid.cu:55-549,
+// also tiles the plane with cells of side >= R and compares adjacent cells;
+// it keeps per-cell pair minima, this kernel a per-slot neighbour table.)
+//
+// Tiles.  Rapidity is tiled over the event's range (clamped to [-15, 15]; a
+// particle outside goes to the edge tile, which keeps the tile index monotone
+// in rapidity), azimuth over [0, 2pi) with wrap-around.  Both sides are at
+// least R (1 + 1e-4) + 1e-5, so two pseudojets closer than that lie in the
+// same or in adjacent tiles; tile indices come from the exact FP64
+// coordinates.  Slots never move (the new jet of a merge takes the slot
+// a = min(c, j)), so the label of a slot (the lowest input index among its
+// constituents) is the slot index itself.
+//
+// Why windows give the same winner as the all-pairs rule.  Let nn'(s) be the
+// nearest neighbour of s within its window, key'(s) its key.  If the global
+// nearest neighbour of s lies outside the window, every other pseudojet is at
+// dR > R (1 + 1e-4) from s, so every pair distance of s exceeds the smaller
+// of the two weights (also after rounding).  Then (i) if s wins the all-pairs
+// argmin its key is the beam distance w_s (a pair key w_t dR^2/R^2 would
+// exceed w_t >= key(t)), and every window candidate u has w_u >= w_s
+// (otherwise key(u) <= w_u < w_s), so key'(s) = w_s as well; (ii) any other
+// such s has key'(s) = w_s >= key(s), or key'(s) = w_u dR^2/R^2 > w_u >=
+// key(u) for its window neighbour u, so it cannot undercut the winner.
+// Pseudojets whose nearest neighbour is inside the window have identical
+// keys in both rules.  Hence, with the same (key, label) order, the windowed
+// argmin selects the same pseudojet, kind and partner as the all-pairs rule
+// at every step.  Each candidate set must be exactly the window, so that a
+// change of one pseudojet is seen by every slot whose neighbour it can be.
+//
+// Tile lists.  Per tile, a list of member slots with kTileSlack free entries
+// after the live ones.  Removal writes a tombstone (-1) in place; a new jet
+// that changes tile is appended.  A reader running concurrently with these
+// updates sees either the old or the new word of any entry, and every reader
+// skips the slots involved in the merge by name, so no reader needs the
+// update to be finished.  The lists are rebuilt (tombstones squeezed out,
+// slack restored) every kTileSlack steps; at most one entry is appended per
+// step.
+//
+// Per step (T = 256 threads, 8 warps):
+//   S1  argmin over the tile summaries (smallest klo, its slot and khi,
+//       second smallest klo), certified as in the small-event kernel,
+//       otherwise an exact argmin over the contenders.                    B1
+//   S2  warps 0-2 merge or promote (the new jet's kinematics and tile);
+//       warps 3-7 find the slots whose neighbour was c or j (in the windows
+//       of c's and j's tiles) and scan the first 32 of them.               B2
+//   S3a thread 0 updates the tile lists; the warps finish the targets'
+//       neighbours, adding the new jet when it lies in their window.      B3
+//       (targets beyond the listed ones: a second pass, then a barrier)
+//   S3b every slot of the new jet's window is compared with it.           B4
+//   S3c warp 0 resolves the new jet's neighbour and then re-summarises its
+//       tile; the other warps re-summarise the other changed tiles.       B5
+#pragma once
+
+#include "fjg_cluster.cuh"
+
+namespace fjg {
+
+constexpr int kTiledT = 256;
+constexpr int kTileSlack = 64;
+constexpr int kMaxTiles = 4096;
+constexpr int kMaxWindowTiles = 9;
+constexpr int kMaxListed = 4 * kMaxTargets;  // targets recorded in S2
+constexpr int kMaxDirty = 64;
+constexpr int kLargeWsBytesPerParticle = 96;  // bound of large_ws_bytes(N) / N for N > 2048
+
+// Summary of one tile: the smallest key lower bound among its members, the
+// member holding it (lowest slot among equal bounds) with its key upper
+// bound, and the second smallest lower bound.
+struct alignas(16) TileSum {
+  float m1;
+  int slot;
+  float u1;
+  float m2;
+};
+
+// Per-event large workspace: pointers into the event's region of
+// large_ws_bytes(N) bytes.
+struct LargeWs {
+  float *rap32, *phi32, *wlo, *whi, *nlo, *nhi, *klo, *khi;  // [N]
+  int *nn, *tile, *pos;                                       // [N]
+  int8_t *pair, *alive;                                       // [N]
+  int* members;                                               // [N + kTileSlack * MT]
+  int *t_start, *t_count;                                     // [MT]
+  TileSum* tsum;                                              // [MT]
+  int max_tiles;                                              // MT
+};
+
+__host__ __device__ __forceinline__ int large_max_tiles(int N) { return (N / 8 < kMaxTiles) ? N / 8 : kMaxTiles; }
+
+__host__ __device__ __forceinline__ int64_t large_ws_bytes(int N) {
+  const int64_t MT = large_max_tiles(N);
+  const int64_t head = 8 * 4 * (int64_t)N + 3 * 4 * (int64_t)N + ((2 * (int64_t)N + 15) & ~(int64_t)15);
+  return head + 4 * ((int64_t)N + kTileSlack * MT) + 2 * 4 * MT + 16 + 16 * MT;
+}
+
+__device__ __forceinline__ LargeWs large_ws(unsigned char* base, int N) {
+  LargeWs L;
+  const int MT = large_max_tiles(N);
+  float* f = reinterpret_cast<float*>(base);
+  L.rap32 = f;
+  L.phi32 = f + N;
+  L.wlo = f + 2 * N;
+  L.whi = f + 3 * N;
+  L.nlo = f + 4 * N;
+  L.nhi = f + 5 * N;
+  L.klo = f + 6 * N;
+  L.khi = f + 7 * N;
+  int* i = reinterpret_cast<int*>(f + 8 * N);
+  L.nn = i;
+  L.tile = i + N;
+  L.pos = i + 2 * N;
+  int8_t* b = reinterpret_cast<int8_t*>(i + 3 * N);
+  L.pair = b;
+  L.alive = b + N;
+  int* m = reinterpret_cast<int*>(b + ((2 * N + 15) & ~15));
+  L.members = m;
+  L.t_start = m + N + kTileSlack * MT;
+  L.t_count = L.t_start + MT;
+  const uintptr_t ts = (reinterpret_cast<uintptr_t>(L.t_count + MT) + 15) & ~uintptr_t(15);
+  L.tsum = reinterpret_cast<TileSum*>(ts);
+  L.max_tiles = MT;
+  return L;
+}
+
+struct TiledShared {
+  static constexpr int W = kTiledT / 32;
+  double rmin, inv_side_r, inv_side_phi;
+  int nrap, nphi, nt;
+  int ta_u, ta_v;  // tile of the new jet (rapidity and azimuth index)
+  Cert warg[W];
+  Arg wexact[W];
+  Cert wcert[W];
+  Cert rcert[kMaxTargets][W];
+  int rlist[kMaxListed];
+  int n_rescan;
+  int dirty[kMaxDirty];
+  int n_dirty;
+  unsigned dirty_bits[kMaxTiles / 32];
+  int event, ctl_njets;
+  double red[3][W];
+  int scan_tmp[W];
+};
+
+__device__ __forceinline__ int tile_u(const TiledShared& S, double rap) {
+  const int u = (int)floor((rap - S.rmin) * S.inv_side_r);
+  return u < 0 ? 0 : (u >= S.nrap ? S.nrap - 1 : u);
+}
+
+__device__ __forceinline__ int tile_v(const TiledShared& S, double phi) {
+  const int v = (int)floor(phi * S.inv_side_phi);
+  return v < 0 ? 0 : (v >= S.nphi ? S.nphi - 1 : v);
+}
+
+// The distinct tiles of the 3x3 window around tile t.
+__device__ __forceinline__ int window_tiles(const TiledShared& S, int t, int* out) {
+  const int u = t / S.nphi, v = t - u * S.nphi;
+  int k = 0;
+  for (int du = -1; du <= 1; ++du) {
+    const int uu = u + du;
+    if (uu < 0 || uu >= S.nrap) continue;
+    if (S.nphi <= 3) {
+      for (int vv = 0; vv < S.nphi; ++vv) out[k++] = uu * S.nphi + vv;
+    } else {
+      for (int dv = -1; dv <= 1; ++dv) {
+        int vv = v + dv;
+        vv = vv < 0 ? vv + S.nphi : (vv >= S.nphi ? vv - S.nphi : vv);
+        out[k++] = uu * S.nphi + vv;
+      }
+    }
+  }
+  return k;
+}
+
+// Union of the windows of tiles t1 and t2 (t2 < 0: t1's window only).
+__device__ __forceinline__ int window_union(const TiledShared& S, int t1, int t2, int* out) {
+  int nw = window_tiles(S, t1, out);
+  if (t2 >= 0 && t2 != t1) {
+    int more[kMaxWindowTiles];
+    const int nm = window_tiles(S, t2, more);
+    for (int k = 0; k < nm; ++k) {
+      bool dup = false;
+      for (int q = 0; q < kMaxWindowTiles; ++q) dup |= (q < nw && out[q] == more[k]);
+      if (!dup) out[nw++] = more[k];
+    }
+  }
+  return nw;
+}
+
+__device__ __forceinline__ bool tiles_adjacent(const TiledShared& S, int t1, int t2) {
+  const int u1 = t1 / S.nphi, u2 = t2 / S.nphi;
+  if (abs(u1 - u2) > 1) return false;
+  if (S.nphi <= 3) return true;
+  const int dv = abs((t1 - u1 * S.nphi) - (t2 - u2 * S.nphi));
+  return dv <= 1 || dv == S.nphi - 1;
+}
+
+__device__ __forceinline__ double dr2_ws(const Ws& g, int s, int t) {
+  return dr2_64(g.at(kRap, s), g.at(kPhi, s), g.at(kRap, t), g.at(kPhi, t));
+}
+
+// Key interval (or exact key) of slot t from its neighbour and distance interval.
+__device__ __forceinline__ void set_key_large(const LargeWs& L, const EventCtx& X, int t) {
+  const int nn = L.nn[t];
+  if (nn < 0) {
+    L.klo[t] = L.wlo[t];
+    L.khi[t] = L.whi[t];
+    L.pair[t] = 0;
+    return;
+  }
+  float klo, khi;
+  const int kind = key_interval(L.wlo[t], L.whi[t], L.wlo[nn], L.whi[nn], L.nlo[t], L.nhi[t], X.ilo, X.ihi, klo, khi);
+  if (kind >= 0) {
+    L.klo[t] = klo;
+    L.khi[t] = khi;
+    L.pair[t] = (int8_t)kind;
+    return;
+  }
+  const double wt = X.g.at(kW, t);
+  const double dp = pair_distance(wt, X.g.at(kW, nn), dr2_ws(X.g, t, nn), X.inv_r2);
+  const bool is_pair = dp < wt;
+  const double key = is_pair ? dp : wt;
+  L.pair[t] = is_pair ? 1 : 0;
+  L.klo[t] = fjk_to_f32(key, 1);
+  L.khi[t] = fjk_to_f32(key, 2);
+}
+
+__device__ __forceinline__ double exact_key_large(const LargeWs& L, const EventCtx& X, int t) {
+  if (!L.pair[t]) return L.klo[t] == L.khi[t] ? (double)L.klo[t] : X.g.at(kW, t);
+  const int nn = L.nn[t];
+  return pair_distance(X.g.at(kW, t), X.g.at(kW, nn), dr2_ws(X.g, t, nn), X.inv_r2);
+}
+
+// Certificate partial of slot t's nearest neighbour over the window of its
+// tile, visited by `nthreads` threads starting at `first`; slots t, skip1 and
+// skip2 and tombstones are skipped.
+__device__ __forceinline__ void window_cert(const TiledShared& S, const LargeWs& L, const EventCtx& X, int t,
+                                            int first, int nthreads, int skip1, int skip2, Cert& c) {
+  int tiles[kMaxWindowTiles];
+  const int nw = window_tiles(S, L.tile[t], tiles);
+  const float rt = L.rap32[t], pt = L.phi32[t];
+  for (int k = 0; k < nw; ++k) {
+    const int tt = tiles[k];
+    const int base = L.t_start[tt], m = L.t_count[tt];
+    for (int i = first; i < m; i += nthreads) {
+      const int u = L.members[base + i];
+      if (u < 0 || u == t || u == skip1 || u == skip2) continue;
+      float lo, hi;
+      dr2_32(rt, pt, L.rap32[u], L.phi32[u], X.bd, lo, hi);
+      cert_add(c, lo, hi, u);
+    }
+  }
+}
+
+// Slot t's neighbour from a combined certificate over the same candidates
+// (window minus skip1/skip2, plus `extra` when >= 0).  Near-ties are settled
+// in FP64 with the lowest slot first.  Whole warp.
+__device__ __forceinline__ int resolve_large(const TiledShared& S, const LargeWs& L, const EventCtx& X, int t,
+                                             const Cert& c, int skip1, int skip2, int extra, float& lo_out,
+                                             float& hi_out) {
+  if (c.i1 < 0) {
+    lo_out = hi_out = __int_as_float(0x7f800000);
+    return -1;
+  }
+  if (cert_ok(c)) {
+    lo_out = c.m1;
+    hi_out = c.u1;
+    return c.i1;
+  }
+  const int lane = threadIdx.x & 31;
+  unsigned long long bk = ~0ull;
+  int bi = 0x7fffffff;
+  const float rt = L.rap32[t], pt = L.phi32[t];
+  auto consider = [&](int u) {
+    float lo, hi;
+    dr2_32(rt, pt, L.rap32[u], L.phi32[u], X.bd, lo, hi);
+    if (lo <= c.u1) {
+      const unsigned long long k = dbits(dr2_ws(X.g, t, u));
+      if (arg_less(k, u, bk, bi)) {
+        bk = k;
+        bi = u;
+      }
+    }
+  };
+  int tiles[kMaxWindowTiles];
+  const int nw = window_tiles(S, L.tile[t], tiles);
+  for (int k = 0; k < nw; ++k) {
+    const int tt = tiles[k];
+    const int base = L.t_start[tt], m = L.t_count[tt];
+    for (int i = lane; i < m; i += 32) {
+      const int u = L.members[base + i];
+      if (u >= 0 && u != t && u != skip1 && u != skip2 && u != extra) consider(u);
+    }
+  }
+  if (extra >= 0 && lane == 0) consider(extra);
+  const Arg r = arg_warp(bk, bi, bi);
+  const double d = __longlong_as_double((long long)r.key);
+  lo_out = fjk_to_f32(d, 1);
+  hi_out = fjk_to_f32(d, 2);
+  return r.idx;
+}
+
+// Summary of tile tt (whole warp).
+__device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
+  const int lane = threadIdx.x & 31;
+  Cert c = cert_empty();
+  const int base = L.t_start[tt], m = L.t_count[tt];
+  for (int i = lane; i < m; i += 32) {
+    const int u = L.members[base + i];
+    if (u < 0) continue;
+    const float lo = L.klo[u];
+    if (lo < c.m1 || (lo == c.m1 && (unsigned)u < (unsigned)c.i1)) {
+      c.m2 = c.m1;
+      c.m1 = lo;
+      c.u1 = L.khi[u];
+      c.i1 = u;
+    } else {
+      c.m2 = fminf(c.m2, lo);
+    }
+  }
+  const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(c.m1));
+  const bool at_min = __float_as_uint(c.m1) == mb && c.i1 >= 0;
+  const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)c.i1 : 0xffffffffu);
+  const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)c.i1 == sb);
+  const int src = ball ? __ffs(ball) - 1 : 0;
+  const float u1 = __shfl_sync(kFull, c.u1, src);
+  const unsigned other = (ball && lane == src) ? __float_as_uint(c.m2) : __float_as_uint(c.m1);
+  const float m2 = __uint_as_float(__reduce_min_sync(kFull, other));
+  if (lane == 0) L.tsum[tt] = TileSum{__uint_as_float(mb), ball ? (int)sb : -1, u1, m2};
+}
+
+// Block-wide rebuild of the tile lists from the live slots (kTileSlack free
+// entries per tile, filled with tombstones) and of every tile summary.
+__device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N) {
+  constexpr int W = kTiledT / 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int t = tid; t < S.nt; t += kTiledT) L.t_count[t] = 0;
+  __syncthreads();
+  for (int s = tid; s < N; s += kTiledT)
+    if (L.alive[s]) atomicAdd(&L.t_count[L.tile[s]], 1);
+  __syncthreads();
+  // exclusive scan of (count + slack) over the tiles, kTiledT at a time
+  int carry = 0;
+  for (int base = 0; base < S.nt; base += kTiledT) {
+    const int t = base + tid;
+    const int v = (t < S.nt) ? L.t_count[t] + kTileSlack : 0;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int x = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += x;
+    }
+    if (lane == 31) S.scan_tmp[warp] = incl;
+    __syncthreads();
+    int wpre = 0, total = 0;
+    for (int k = 0; k < W; ++k) {
+      if (k < warp) wpre += S.scan_tmp[k];
+      total += S.scan_tmp[k];
+    }
+    if (t < S.nt) {
+      L.t_start[t] = carry + wpre + incl - v;
+      L.t_count[t] = 0;
+    }
+    carry += total;
+    __syncthreads();
+  }
+  for (int s = tid; s < N; s += kTiledT) {
+    if (!L.alive[s]) continue;
+    const int t = L.tile[s];
+    const int p = atomicAdd(&L.t_count[t], 1);
+    L.members[L.t_start[t] + p] = s;
+    L.pos[s] = p;
+  }
+  __syncthreads();
+  for (int t = warp; t < S.nt; t += W) {
+    const int end = L.t_start[t] + L.t_count[t];
+    for (int i = lane; i < kTileSlack; i += 32) L.members[end + i] = -1;
+  }
+  __syncthreads();
+  for (int t = warp; t < S.nt; t += W) tile_summary(L, t);
+  __syncthreads();
+}
+
+__device__ __forceinline__ void mark_dirty(TiledShared& S, int t) {
+  const unsigned bit = 1u << (t & 31);
+  const unsigned old = atomicOr(&S.dirty_bits[t >> 5], bit);
+  if (!(old & bit)) {
+    const int k = atomicAdd(&S.n_dirty, 1);
+    if (k < kMaxDirty) S.dirty[k] = t;
+  }
+}
+
+// A whole warp rescans slot t's window (lists up to date) and stores its
+// neighbour and key.
+__device__ __forceinline__ void rescan_warp(TiledShared& S, const LargeWs& L, const EventCtx& X, int t, int skip) {
+  const int lane = threadIdx.x & 31;
+  Cert x = cert_empty();
+  window_cert(S, L, X, t, lane, 32, skip, -1, x);
+  x = cert_warp(x);
+  float lo, hi;
+  const int nn = resolve_large(S, L, X, t, x, skip, -1, -1, lo, hi);
+  if (lane == 0) {
+    L.nn[t] = nn;
+    L.nlo[t] = lo;
+    L.nhi[t] = hi;
+    set_key_large(L, X, t);
+    mark_dirty(S, L.tile[t]);
+  }
+  __syncwarp();
+}
+
+__device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, unsigned char* large_base, int e) {
+  constexpr int T = kTiledT;
+  constexpr int W = T / 32;
+  constexpr int MW = 3;
+  constexpr int TR = T - 32 * MW;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t off = A.offsets[e];
+  EventCtx X;
+  X.N = (int)(A.offsets[e + 1] - off);
+  X.algo = A.algo ? A.algo[e] : A.algo_all;
+  const double R = A.radius ? A.radius[e] : A.r_all;
+  X.inv_r2 = 1.0 / (R * R);
+  X.ilo = fjk_to_f32(X.inv_r2, 1);
+  X.ihi = fjk_to_f32(X.inv_r2, 2);
+  X.g.base = A.ws + off;
+  X.g.stride = A.ws_stride;
+  const Ws& g = X.g;
+  const int N = X.N;
+  // event e's region starts kLargeWsBytesPerParticle * offsets[e] bytes in
+  const LargeWs L = large_ws(large_base + off * kLargeWsBytesPerParticle, N);
+
+  // ---- load and kinematics; rapidity range
+  double rlo = 1e300, rhi = -1e300, amax = 0.0;
+  for (int s = tid; s < N; s += T) {
+    const double* p = A.p4 + (off + s) * A.p4_stride;
+    const double px = p[0], py = p[1], pz = p[2], E = p[3];
+    const Kin kin = kinematics(px, py, pz, E, X.algo);
+    g.at(kPx, s) = px;
+    g.at(kPy, s) = py;
+    g.at(kPz, s) = pz;
+    g.at(kE, s) = E;
+    g.at(kRap, s) = kin.rap;
+    g.at(kPhi, s) = kin.phi;
+    g.at(kW, s) = kin.w;
+    L.rap32[s] = fjk_to_f32(kin.rap, 0);
+    L.phi32[s] = fjk_to_f32(kin.phi, 0);
+    L.wlo[s] = fjk_to_f32(kin.w, 1);
+    L.whi[s] = fjk_to_f32(kin.w, 2);
+    L.alive[s] = 1;
+    rlo = fmin(rlo, kin.rap);
+    rhi = fmax(rhi, kin.rap);
+    amax = fmax(amax, fabs(kin.rap));
+    if (A.owner) A.owner[off + s] = s;  // union-find parent by label
+  }
+  for (int o = 16; o; o >>= 1) {
+    rlo = fmin(rlo, __shfl_xor_sync(kFull, rlo, o));
+    rhi = fmax(rhi, __shfl_xor_sync(kFull, rhi, o));
+    amax = fmax(amax, __shfl_xor_sync(kFull, amax, o));
+  }
+  if (lane == 0) {
+    S.red[0][warp] = rlo;
+    S.red[1][warp] = rhi;
+    S.red[2][warp] = amax;
+  }
+  for (int k = tid; k < kMaxTiles / 32; k += T) S.dirty_bits[k] = 0;
+  __syncthreads();
+  if (tid == 0) {
+    double lo = 1e300, hi = -1e300;
+    for (int k = 0; k < W; ++k) {
+      lo = fmin(lo, S.red[0][k]);
+      hi = fmax(hi, S.red[1][k]);
+    }
+    lo = fmax(lo, -15.0);
+    hi = fmin(hi, 15.0);
+    if (!(hi >= lo)) hi = lo;
+    const double side_min = R * (1.0 + 1e-4) + 1e-5;
+    int nphi = (int)fmin(floor(6.283185307179586 / side_min), 4096.0);
+    nphi = nphi < 1 ? 1 : nphi;
+    int nrap = (int)fmin(floor((hi - lo) / side_min), 4096.0);
+    nrap = nrap < 1 ? 1 : nrap;
+    // coarser tiles are still correct, only slower
+    while (nrap * nphi > L.max_tiles) {
+      if (nrap > 1)
+        nrap = (nrap + 1) / 2;
+      else
+        nphi = (nphi + 1) / 2;
+    }
+    S.nrap = nrap;
+    S.nphi = nphi;
+    S.nt = nrap * nphi;
+    S.rmin = lo;
+    S.inv_side_r = (double)nrap / fmax(hi - lo, side_min);
+    S.inv_side_phi = (double)nphi / 6.283185307179586;
+    S.ctl_njets = 0;
+    S.n_rescan = 0;
+    S.n_dirty = 0;
+  }
+  {
+    double rmax = 0.0;
+    for (int k = 0; k < W; ++k) rmax = fmax(rmax, S.red[2][k]);
+    X.bd = make_bound(rmax);
+  }
+  __syncthreads();
+  for (int s = tid; s < N; s += T) L.tile[s] = tile_u(S, g.at(kRap, s)) * S.nphi + tile_v(S, g.at(kPhi, s));
+  __syncthreads();
+  rebuild_tiles(S, L, N);  // (summaries are recomputed once the keys exist)
+
+  // ---- initial nearest neighbours within the windows
+  for (int t = tid; t < N; t += T) {
+    Cert c = cert_empty();
+    window_cert(S, L, X, t, 0, 1, -1, -1, c);
+    int nn = c.i1;
+    float nlo = c.m1, nhi = c.u1;
+    if (nn >= 0 && !cert_ok(c)) {
+      unsigned long long bk = ~0ull;
+      int bi = 0x7fffffff;
+      int tiles[kMaxWindowTiles];
+      const int nw = window_tiles(S, L.tile[t], tiles);
+      const float rt = L.rap32[t], pt = L.phi32[t];
+      for (int k = 0; k < nw; ++k) {
+        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
+        for (int i = 0; i < m; ++i) {
+          const int u = L.members[base + i];
+          if (u < 0 || u == t) continue;
+          float lo, hi;
+          dr2_32(rt, pt, L.rap32[u], L.phi32[u], X.bd, lo, hi);
+          if (lo <= c.u1) {
+            const unsigned long long du = dbits(dr2_ws(g, t, u));
+            if (arg_less(du, u, bk, bi)) {
+              bk = du;
+              bi = u;
+            }
+          }
+        }
+      }
+      nn = bi;
+      const double d = __longlong_as_double((long long)bk);
+      nlo = fjk_to_f32(d, 1);
+      nhi = fjk_to_f32(d, 2);
+    }
+    L.nn[t] = nn;
+    L.nlo[t] = nlo;
+    L.nhi[t] = nhi;
+  }
+  __syncthreads();
+  for (int t = tid; t < N; t += T) set_key_large(L, X, t);
+  __syncthreads();
+  for (int t = warp; t < S.nt; t += W) tile_summary(L, t);
+  __syncthreads();
+
+  // ---- clustering steps
+  int n = N;
+  int step = 0;
+  while (n > 0) {
+    if (step > 0 && step % kTileSlack == 0) rebuild_tiles(S, L, N);
+
+    // S1: argmin over the tile summaries (slot order breaks ties)
+    Cert mine = cert_empty();
+    for (int t = tid; t < S.nt; t += T) {
+      const TileSum ts = L.tsum[t];
+      if (ts.m1 < mine.m1 || (ts.m1 == mine.m1 && (unsigned)ts.slot < (unsigned)mine.i1)) {
+        mine.m2 = fminf(mine.m1, ts.m2);
+        mine.m1 = ts.m1;
+        mine.u1 = ts.u1;
+        mine.i1 = ts.slot;
+      } else {
+        mine.m2 = fminf(mine.m2, ts.m1);
+      }
+    }
+    {
+      const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(mine.m1));
+      const bool at_min = __float_as_uint(mine.m1) == mb && mine.i1 >= 0;
+      const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)mine.i1 : 0xffffffffu);
+      const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)mine.i1 == sb);
+      const int src = ball ? __ffs(ball) - 1 : 0;
+      Cert wc;
+      wc.m1 = __uint_as_float(mb);
+      wc.i1 = ball ? (int)sb : -1;
+      wc.u1 = __shfl_sync(kFull, mine.u1, src);
+      const unsigned other = (ball && lane == src) ? __float_as_uint(mine.m2) : __float_as_uint(mine.m1);
+      wc.m2 = __uint_as_float(__reduce_min_sync(kFull, other));
+      if (lane == 0) S.warg[warp] = wc;
+    }
+    __syncthreads();  // B1
+    int c;
+    {
+      const Cert x = (lane < W) ? S.warg[lane] : cert_empty();
+      const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(x.m1));
+      const bool at_min = __float_as_uint(x.m1) == mb && x.i1 >= 0;
+      const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)x.i1 : 0xffffffffu);
+      const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)x.i1 == sb);
+      const int src = ball ? __ffs(ball) - 1 : 0;
+      c = ball ? (int)sb : -1;
+      const float u1 = __shfl_sync(kFull, x.u1, src);
+      const unsigned other = (ball && lane == src) ? __float_as_uint(x.m2) : __float_as_uint(x.m1);
+      const float m2 = __uint_as_float(__reduce_min_sync(kFull, other));
+      if (c >= 0 && !(u1 < m2)) {
+        // near-tie: exact keys of every slot whose lower bound is <= u1
+        unsigned long long bk = ~0ull;
+        int bi = 0x7fffffff;
+        for (int tt = warp; tt < S.nt; tt += W) {
+          if (!(L.tsum[tt].m1 <= u1)) continue;
+          const int base = L.t_start[tt], m = L.t_count[tt];
+          for (int i = lane; i < m; i += 32) {
+            const int t = L.members[base + i];
+            if (t >= 0 && L.klo[t] <= u1) {
+              const unsigned long long kk = dbits(exact_key_large(L, X, t));
+              if (arg_less(kk, t, bk, bi)) {
+                bk = kk;
+                bi = t;
+              }
+            }
+          }
+        }
+        const Arg wa = arg_warp(bk, bi, bi);
+        if (lane == 0) S.wexact[warp] = wa;
+        __syncthreads();
+        const Arg y = (lane < W) ? S.wexact[lane] : Arg{~0ull, 0x7fffffff, -1};
+        c = arg_warp(y.key, y.label, y.idx).idx;
+        __syncthreads();
+      }
+    }
+    if (c < 0) {
+      if (tid == 0) atomicOr(A.status, 4);
+      break;
+    }
+
+    // S2
+    const bool pair = L.pair[c] != 0 && L.nn[c] >= 0;
+    const int j = pair ? L.nn[c] : -1;
+    const int a = pair ? min(c, j) : -1;
+    const int b = pair ? max(c, j) : c;
+    const int tile_c = L.tile[c], tile_j = pair ? L.tile[j] : -1;
+
+    if (warp < MW) {
+      double pxc = 0, pyc = 0, pzc = 0, Ec = 0, pxj = 0, pyj = 0, pzj = 0, Ej = 0;
+      double rc = 0, fc = 0, wc = 0, rj = 0, fj = 0, wj = 0;
+      if (lane == 0) {
+        pxc = g.at(kPx, c);
+        pyc = g.at(kPy, c);
+        pzc = g.at(kPz, c);
+        Ec = g.at(kE, c);
+        wc = g.at(kW, c);
+        if (pair) {
+          pxj = g.at(kPx, j);
+          pyj = g.at(kPy, j);
+          pzj = g.at(kPz, j);
+          Ej = g.at(kE, j);
+          wj = g.at(kW, j);
+          rc = g.at(kRap, c);
+          fc = g.at(kPhi, c);
+          rj = g.at(kRap, j);
+          fj = g.at(kPhi, j);
+        }
+      }
+      __syncwarp();
+      named_sync(2, 32 * MW);  // every merge warp has read c and j
+      if (pair) {
+        const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
+        if (lane == 0 && warp == 0) {
+          const double phi = fjk_phi(px, py);
+          g.at(kPhi, a) = phi;
+          L.phi32[a] = fjk_to_f32(phi, 0);
+          S.ta_v = tile_v(S, phi);
+        }
+        if (lane == 0 && warp == 1) {
+          const double pz = __dadd_rn(pzc, pzj), E = __dadd_rn(Ec, Ej);
+          const double rap = fjk_rap(px, py, pz, E);
+          g.at(kPx, a) = px;
+          g.at(kPy, a) = py;
+          g.at(kPz, a) = pz;
+          g.at(kE, a) = E;
+          g.at(kRap, a) = rap;
+          L.rap32[a] = fjk_to_f32(rap, 0);
+          S.ta_u = tile_u(S, rap);
+        }
+        if (lane == 0 && warp == 2) {
+          const double w = fjk_weight(px, py, X.algo);
+          g.at(kW, a) = w;
+          L.wlo[a] = fjk_to_f32(w, 1);
+          L.whi[a] = fjk_to_f32(w, 2);
+          const double d = pair_distance(wc, wj, dr2_64(rc, fc, rj, fj), X.inv_r2);
+          if (A.history) A.history[off + step] = StepRec{a, b, d};
+          if (A.owner) A.owner[off + b] = a;
+        }
+      } else if (lane == 0 && warp == 2) {
+        const int nj = S.ctl_njets;
+        double* jo = A.jets + (off + nj) * 4;
+        jo[0] = pxc;
+        jo[1] = pyc;
+        jo[2] = pzc;
+        jo[3] = Ec;
+        A.jet_label[off + nj] = c;
+        if (A.history) A.history[off + step] = StepRec{c, -1, wc};
+        if (A.owner) A.owner[off + c] = -(nj + 1);
+        S.ctl_njets = nj + 1;
+      }
+      __syncwarp();
+    } else {
+      // targets: live slots other than c, j whose neighbour is c or j; they
+      // lie in the windows of c's and j's tiles
+      const int r0 = tid - 32 * MW;
+      int tiles[2 * kMaxWindowTiles];
+      const int nw = window_union(S, tile_c, tile_j, tiles);
+      for (int k = 0; k < nw; ++k) {
+        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
+        for (int i = r0; i < m; i += TR) {
+          const int u = L.members[base + i];
+          if (u < 0 || u == c || u == j) continue;
+          const int nu = L.nn[u];
+          if (nu == c || (pair && nu == j)) {
+            const int p = atomicAdd(&S.n_rescan, 1);
+            if (p < kMaxListed) S.rlist[p] = u;
+          }
+        }
+      }
+      named_sync(1, TR);
+      const int nr = min(S.n_rescan, kMaxTargets);
+      for (int r = 0; r < nr; ++r) {
+        Cert rc = cert_empty();
+        window_cert(S, L, X, S.rlist[r], r0, TR, c, j, rc);
+        const Cert wc = cert_warp(rc);
+        if (lane == 0) S.rcert[r][warp] = wc;
+      }
+    }
+    __syncthreads();  // B2
+    --n;
+    ++step;
+    if (n == 0) break;
+    const int n_found = S.n_rescan;
+    const int nr_all = min(n_found, kMaxListed);
+    const int nr = min(nr_all, kMaxTargets);
+    const int ta = pair ? S.ta_u * S.nphi + S.ta_v : -1;
+
+    // S3a: tile lists (thread 0: a tombstone for b, and for a when it
+    // changes tile, then an append); targets (one warp each)
+    if (tid == 0) {
+      L.members[L.t_start[L.tile[b]] + L.pos[b]] = -1;
+      L.alive[b] = 0;
+      mark_dirty(S, L.tile[b]);
+      if (pair) {
+        const int told = L.tile[a];
+        mark_dirty(S, told);
+        if (ta != told) {
+          L.members[L.t_start[told] + L.pos[a]] = -1;
+          const int p = L.t_count[ta];
+          L.members[L.t_start[ta] + p] = a;
+          L.pos[a] = p;
+          L.tile[a] = ta;
+          L.t_count[ta] = p + 1;
+          mark_dirty(S, ta);
+        }
+      }
+    }
+    for (int r = warp; r < nr_all; r += W) {
+      const int t = S.rlist[r];
+      Cert x = cert_empty();
+      if (r < nr)
+        x = (lane >= MW && lane < W) ? S.rcert[r][lane] : cert_empty();
+      else
+        window_cert(S, L, X, t, lane, 32, c, j, x);
+      const int extra = (pair && tiles_adjacent(S, L.tile[t], ta)) ? a : -1;
+      if (extra >= 0 && lane == 0) {
+        float lo, hi;
+        dr2_32(L.rap32[t], L.phi32[t], L.rap32[a], L.phi32[a], X.bd, lo, hi);
+        cert_add(x, lo, hi, a);
+      }
+      x = cert_warp(x);
+      float lo, hi;
+      const int nn = resolve_large(S, L, X, t, x, c, j, extra, lo, hi);
+      if (lane == 0) {
+        L.nn[t] = nn;
+        L.nlo[t] = lo;
+        L.nhi[t] = hi;
+        set_key_large(L, X, t);
+        mark_dirty(S, L.tile[t]);
+      }
+      __syncwarp();
+    }
+    __syncthreads();  // B3: lists updated, listed targets done
+    if (n_found > kMaxListed) {
+      // more targets than listed (degenerate inputs, e.g. repeated
+      // particles): find them again with the lists up to date; the listed
+      // ones are found too and get the same answer again
+      int tiles[2 * kMaxWindowTiles];
+      const int nw = window_union(S, tile_c, tile_j, tiles);
+      for (int k = warp; k < nw; k += W) {
+        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
+        for (int i0 = 0; i0 < m; i0 += 32) {
+          const int i = i0 + lane;
+          const int u = (i < m) ? L.members[base + i] : -1;
+          const bool hit = u >= 0 && u != a && u != b && (L.nn[u] == c || (pair && L.nn[u] == j));
+          unsigned ball = __ballot_sync(kFull, hit);
+          while (ball) {
+            const int src = __ffs(ball) - 1;
+            ball &= ball - 1;
+            rescan_warp(S, L, X, __shfl_sync(kFull, u, src), b);
+          }
+        }
+      }
+      __syncthreads();
+    }
+
+    // S3b: every slot of the new jet's window against the new jet
+    if (pair) {
+      Cert ca = cert_empty();
+      int tiles[kMaxWindowTiles];
+      const int nw = window_tiles(S, ta, tiles);
+      const float ra = L.rap32[a], pa = L.phi32[a];
+      for (int k = 0; k < nw; ++k) {
+        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
+        for (int i = tid; i < m; i += T) {
+          const int t = L.members[base + i];
+          if (t < 0 || t == a || t == b) continue;
+          float lo, hi;
+          dr2_32(L.rap32[t], L.phi32[t], ra, pa, X.bd, lo, hi);
+          cert_add(ca, lo, hi, t);
+          const int cn = L.nn[t];
+          if (cn == a) continue;
+          bool closer;
+          float ulo = lo, uhi = hi;
+          if (cn < 0 || hi < L.nlo[t]) {
+            closer = true;
+          } else if (lo > L.nhi[t]) {
+            closer = false;
+          } else {
+            const double da = dr2_ws(g, t, a);
+            const double dc = dr2_ws(g, t, cn);
+            closer = da < dc || (da == dc && a < cn);
+            ulo = fjk_to_f32(da, 1);
+            uhi = fjk_to_f32(da, 2);
+          }
+          if (closer) {
+            L.nn[t] = a;
+            L.nlo[t] = ulo;
+            L.nhi[t] = uhi;
+            set_key_large(L, X, t);
+            mark_dirty(S, tiles[k]);
+          }
+        }
+      }
+      const Cert wc = cert_warp(ca);
+      if (lane == 0) S.wcert[warp] = wc;
+    }
+    __syncthreads();  // B4
+    // S3c: the new jet's neighbour (warp 0, then its tile's summary) and the
+    // other changed tiles' summaries (the remaining warps)
+    const int nd = S.n_dirty;
+    if (pair && warp == 0) {
+      Cert x = (lane < W) ? S.wcert[lane] : cert_empty();
+      x = cert_warp(x);
+      float lo, hi;
+      const int nn = resolve_large(S, L, X, a, x, b, -1, -1, lo, hi);
+      if (lane == 0) {
+        L.nn[a] = nn;
+        L.nlo[a] = lo;
+        L.nhi[a] = hi;
+        set_key_large(L, X, a);
+      }
+      __syncwarp();
+      tile_summary(L, ta);
+    }
+    if (!(pair && warp == 0)) {
+      const int w0 = pair ? 1 : 0;  // warps taking part: w0 .. W-1
+      if (nd > kMaxDirty) {
+        for (int t = warp - w0; t < S.nt; t += W - w0)
+          if (t != ta) tile_summary(L, t);
+      } else {
+        for (int k = warp - w0; k < nd; k += W - w0)
+          if (S.dirty[k] != ta) tile_summary(L, S.dirty[k]);
+      }
+    }
+    __syncthreads();  // B5
+    if (nd > kMaxDirty) {
+      for (int k = tid; k < kMaxTiles / 32; k += T) S.dirty_bits[k] = 0;
+    } else {
+      for (int k = tid; k < nd; k += T) S.dirty_bits[S.dirty[k] >> 5] = 0;
+    }
+    if (tid == 0) {
+      S.n_rescan = 0;
+      S.n_dirty = 0;
+    }
+    // the next reads of dirty_bits, n_rescan and n_dirty follow B1 and B2
+  }
+
+  // ---- epilogue: jet count, and constituent ownership from the union-find
+  // parents (owner[label] = parent label, or -(jet+1) once promoted)
+  __syncthreads();
+  if (tid == 0) A.n_jets[e] = S.ctl_njets;
+  if (A.owner) {
+    for (int s = tid; s < N; s += T) {
+      int x = s, guard = 0;
+      int v = A.owner[off + x];
+      while (v >= 0 && v != x && guard < N) {
+        x = v;
+        v = A.owner[off + x];
+        ++guard;
+      }
+      L.pos[s] = (v < 0) ? (-v - 1) : -1;
+    }
+    __syncthreads();
+    for (int s = tid; s < N; s += T) A.owner[off + s] = L.pos[s];
+  }
+  __syncthreads();
+}
+
+}  // namespace fjg

@@ -20,22 +20,71 @@ __global__ void __launch_bounds__(T) k_cluster_smem(BatchArgs A) {
   }
 }
 
+// Persistent tiled kernel for events above kSmemMaxN particles.
+__global__ void __launch_bounds__(kTiledT) k_cluster_tiled(BatchArgs A) {
+  __shared__ TiledShared S;
+  const int count = *A.n_order;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int q = atomicAdd(A.queue, 1);
+      S.event = (q < count) ? A.order[q] : -1;
+    }
+    __syncthreads();
+    const int e = S.event;
+    if (e < 0) break;
+    cluster_event_tiled(S, A, A.large_ws, e);  // ends with a barrier
+  }
+}
+
 // Events are handed to the bucket kernels largest first (longest-processing-
 // time order), so that the biggest events do not start last and form the tail.
 // Three passes: a size histogram, a descending scan that also yields each
 // bucket's count, and a scatter into per-bucket lists.  Empty events are
 // finished in the first pass; oversize ones raise the status word.
 
-__global__ void k_size_hist(const int64_t* offsets, int n_events, int32_t* hist, int32_t* n_jets, int* status) {
+// Events above kSmemMaxN particles go straight to the large list (or raise
+// kStatusTooBig when there is no large workspace, or it is too small).
+__global__ void k_size_hist(const int64_t* offsets, int n_events, int32_t* hist, int32_t* n_jets, int* status,
+                            int32_t* large_order, int32_t* large_count, int64_t large_particles) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
     const int64_t n64 = offsets[e + 1] - offsets[e];
-    if (n64 <= 0 || n64 > kSmemMaxN) {
+    if (n64 > kSmemMaxN) {
+      if (n64 <= kLargeMaxN && offsets[e + 1] <= large_particles) {
+        large_order[atomicAdd(large_count, 1)] = e;
+      } else {
+        n_jets[e] = 0;
+        atomicOr(status, kStatusTooBig);
+      }
+      continue;
+    }
+    if (n64 <= 0) {
       n_jets[e] = 0;
       if (n64 < 0) atomicOr(status, kStatusBadArg);
-      if (n64 > kSmemMaxN) atomicOr(status, kStatusTooBig);
       continue;
     }
     atomicAdd(&hist[n64], 1);
+  }
+}
+
+// Largest first within the large list (rank sort in one block; lists longer
+// than kLargeSortMax keep their arrival order, which is only slower).
+constexpr int kLargeSortMax = 4096;
+
+__global__ void __launch_bounds__(1024) k_large_sort(const int64_t* offsets, int32_t* order, const int32_t* count) {
+  __shared__ int32_t ev[kLargeSortMax];
+  __shared__ int32_t sz[kLargeSortMax];
+  const int L = *count;
+  if (L < 2 || L > kLargeSortMax) return;
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    const int e = order[i];
+    ev[i] = e;
+    sz[i] = (int)(offsets[e + 1] - offsets[e]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    int rank = 0;
+    for (int k = 0; k < L; ++k) rank += (sz[k] > sz[i]) || (sz[k] == sz[i] && ev[k] < ev[i]);
+    order[rank] = ev[i];
   }
 }
 
@@ -97,11 +146,34 @@ __global__ void k_size_scatter(const int64_t* offsets, int n_events, int32_t* hi
 static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_events, cudaStream_t stream) {
   cudaError_t err;
   if ((err = cudaMemsetAsync(sc.hist, 0, sizeof(int32_t) * kHistBins, stream)) != cudaSuccess) return err;
-  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumBuckets, stream)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumQueues, stream)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(sc.counts + kLargeQueue, 0, sizeof(int32_t), stream)) != cudaSuccess) return err;
   const int grid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
-  k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status);
+  int32_t* large_order = sc.order + kLargeQueue * sc.cap_events;
+  k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status, large_order,
+                                        sc.counts + kLargeQueue, sc.large_ws ? sc.large_ws_particles : 0);
   k_size_scan<<<1, 1024, 0, stream>>>(sc.hist, sc.counts);
   k_size_scatter<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, sc.order, sc.cap_events);
+  k_large_sort<<<1, 1024, 0, stream>>>(base.offsets, large_order, sc.counts + kLargeQueue);
+  return cudaGetLastError();
+}
+
+// The large list: one CTA per event, at most two per SM (the events are
+// few and long; the small buckets fill the rest of each SM).
+static cudaError_t launch_large(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
+                                cudaStream_t s) {
+  if (!sc.large_ws) return cudaSuccess;
+  BatchArgs A = base;
+  A.order = sc.order + kLargeQueue * sc.cap_events;
+  A.n_order = sc.counts + kLargeQueue;
+  A.queue = sc.queues + kLargeQueue;
+  A.ws = sc.ws;
+  A.ws_stride = sc.ws_stride;
+  A.large_ws = sc.large_ws;
+  int grid = 2 * num_sms;
+  if (grid > n_events) grid = n_events;
+  if (grid < 1) grid = 1;
+  k_cluster_tiled<<<grid, kTiledT, 0, s>>>(A);
   return cudaGetLastError();
 }
 
@@ -158,7 +230,16 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
   cudaError_t err = launch_sort(base, sc, n_events, stream);
   if (err != cudaSuccess) return err;
   if ((err = cudaEventRecord(*ev_fork, stream)) != cudaSuccess) return err;
-  // largest events first: their bucket is launched first
+  // largest events first: their list is launched first
+  {
+    cudaStream_t s = side ? side[kLargeQueue] : stream;
+    if (side && (err = cudaStreamWaitEvent(s, *ev_fork, 0)) != cudaSuccess) return err;
+    if ((err = launch_large(base, sc, n_events, num_sms, s)) != cudaSuccess) return err;
+    if (side) {
+      if ((err = cudaEventRecord(ev_join[kLargeQueue], s)) != cudaSuccess) return err;
+      if ((err = cudaStreamWaitEvent(stream, ev_join[kLargeQueue], 0)) != cudaSuccess) return err;
+    }
+  }
   for (int b = kNumBuckets - 1; b >= 0; --b) {
     cudaStream_t s = side ? side[b] : stream;
     if (side && (err = cudaStreamWaitEvent(s, *ev_fork, 0)) != cudaSuccess) return err;
@@ -184,6 +265,7 @@ cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int
                                    cudaStream_t stream) {
   cudaError_t err = launch_sort(base, sc, n_events, stream);
   if (err != cudaSuccess) return err;
+  if ((err = launch_large(base, sc, n_events, num_sms, stream)) != cudaSuccess) return err;
   for (int b = kNumBuckets - 1; b >= 0; --b) {
     BatchArgs A = base;
     A.order = sc.order + b * sc.cap_events;
@@ -203,7 +285,7 @@ __global__ void k_single_setup(int64_t* offsets1, int32_t* order, int32_t* count
   offsets1[0] = 0;
   offsets1[1] = n;
   order[0] = 0;
-  for (int b = 0; b < kNumBuckets; ++b) {
+  for (int b = 0; b < kNumQueues; ++b) {
     counts[b] = 1;
     queues[b] = 0;
   }
@@ -211,7 +293,7 @@ __global__ void k_single_setup(int64_t* offsets1, int32_t* order, int32_t* count
 
 cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream) {
   const int b = bucket_of(n);
-  if (b < 0) return cudaErrorInvalidValue;
+  if (b < 0 && (!sc.large_ws || n > sc.large_ws_particles || n > kLargeMaxN)) return cudaErrorInvalidValue;
   k_single_setup<<<1, 1, 0, stream>>>(sc.offsets1, sc.order, sc.counts, sc.queues, n);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
@@ -222,6 +304,11 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaS
   A.queue = sc.queues;
   A.ws = sc.ws;
   A.ws_stride = sc.ws_stride;
+  if (b < 0) {
+    A.large_ws = sc.large_ws;
+    k_cluster_tiled<<<1, kTiledT, 0, stream>>>(A);
+    return cudaGetLastError();
+  }
   return launch_bucket_dispatch(b, A, 1, stream);
 }
 

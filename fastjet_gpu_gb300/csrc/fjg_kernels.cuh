@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "fjg_cluster.cuh"
+#include "fjg_cluster_tiled.cuh"
 
 namespace fjg {
 
@@ -13,6 +14,11 @@ namespace fjg {
 // per thread let 8, 8, 4 and 2 CTAs share an SM.
 constexpr int kNumBuckets = 4;
 constexpr int kSmemMaxN = 2048;
+// Events above kSmemMaxN particles form a fifth work list, run by the tiled
+// kernel (one CTA of 256 threads per event, state in the large workspace).
+constexpr int kLargeQueue = kNumBuckets;
+constexpr int kNumQueues = kNumBuckets + 1;
+constexpr int kLargeMaxN = 1 << 24;
 
 __host__ __device__ inline int bucket_of(int n) {
   return n <= 256 ? 0 : n <= 512 ? 1 : n <= 1024 ? 2 : n <= 2048 ? 3 : -1;
@@ -25,30 +31,34 @@ static_assert(sizeof(SmemLayout<256, 8>) <= 232448 / 2, "bucket 3: two CTAs per 
 
 // Device-side batch descriptor scratch owned by a context.
 struct Scratch {
-  int32_t* order;   // [kNumBuckets][cap_events]
-  int32_t* counts;  // [kNumBuckets]
-  int* queues;      // [kNumBuckets]
+  int32_t* order;   // [kNumQueues][cap_events]
+  int32_t* counts;  // [kNumQueues]
+  int* queues;      // [kNumQueues]
   int* status;      // [1]
   int64_t* offsets1;  // [2] single-event offsets {0, n}
   int cap_events;
   double* ws;         // [kWsFields][ws_stride] exact per-particle state
   int64_t ws_stride;  // particles the workspace holds
   int32_t* hist;      // [kHistBins] events per size, then per-size positions (sorting by size)
+  unsigned char* large_ws;    // kLargeWsBytesPerParticle per particle (null: large events are refused)
+  int64_t large_ws_particles;  // particles the large workspace covers
 };
 
 constexpr int kHistBins = kSmemMaxN + 1;
 
-// Launch the bucketing kernel plus one persistent kernel per bucket on
-// `stream` (buckets run concurrently on the side streams when given).
+// Launch the bucketing kernels plus one persistent kernel per work list on
+// `stream` (the lists run concurrently on the kNumQueues side streams when
+// given).
 cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
                          cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join);
 
-// The bucketing kernel and the four bucket kernels, all on `stream` one after
+// The bucketing kernels and the per-list kernels, all on `stream` one after
 // another (no side streams, no events).
 cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
                                    cudaStream_t stream);
 
-// One event, one CTA (the plain per-event-launch path).
+// One event, one CTA (the plain per-event-launch path; the tiled kernel above
+// kSmemMaxN particles).
 cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream);
 
 // Scatter jets into the reference's PseudoJet records (in place).

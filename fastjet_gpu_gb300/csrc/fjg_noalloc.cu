@@ -8,7 +8,8 @@
 // library context, because fjg_ctx_create allocates the context's scratch.
 //
 // How: the bookkeeping the batch kernels need besides their inputs and outputs
-// (per-bucket event lists, work-queue counters, the error word) lives in one
+// (per-list event lists, work-queue counters, the error word, the kernels'
+// per-particle workspaces) lives in one
 // file-scope device array of fixed size, kNoAllocScratchBytes, that every GPU
 // which loads this library holds until the process exits.  The host cannot use
 // the array's name as a device address, so the first call on each device
@@ -32,10 +33,11 @@ constexpr int kNoAllocMaxParticles = FJG_NOALLOC_MAX_PARTICLES;
 
 struct NoAllocScratch {
   double ws[fjg::kWsFields * kNoAllocMaxParticles];    // exact per-particle state (overwritten per event)
-  int32_t order[fjg::kNumBuckets * kNoAllocMaxEvents];  // per-bucket event lists
+  unsigned char large_ws[fjg::kLargeWsBytesPerParticle * kNoAllocMaxParticles];  // tiled-kernel state
+  int32_t order[fjg::kNumQueues * kNoAllocMaxEvents];  // per-list event lists
   int32_t hist[fjg::kHistBins];                        // size histogram (zeroed per call)
-  int32_t counts[fjg::kNumBuckets];                    // events per bucket (zeroed per call)
-  int32_t queues[fjg::kNumBuckets];                    // work-queue heads (zeroed per call)
+  int32_t counts[fjg::kNumQueues];                     // events per list (zeroed per call)
+  int32_t queues[fjg::kNumQueues];                     // work-queue heads (zeroed per call)
   int32_t status;                                      // kernel error bits (zeroed per call)
 };
 
@@ -101,6 +103,8 @@ extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t*
   sc.hist = sc_dev->hist;
   sc.ws = sc_dev->ws;
   sc.ws_stride = kNoAllocMaxParticles;
+  sc.large_ws = sc_dev->large_ws;
+  sc.large_ws_particles = kNoAllocMaxParticles;
 
   fjg::BatchArgs A{};
   A.p4 = p4;

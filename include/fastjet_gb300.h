@@ -145,7 +145,7 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
  * current device and returns after synchronising it.
  * Limits: at most FJG_NOALLOC_MAX_EVENTS events and FJG_NOALLOC_MAX_PARTICLES
  * particles (`total` = offsets[n_events]) per call (larger batches return
- * FJG_EINVAL), events of at most 2048 particles (else FJG_ETOOBIG).  The
+ * FJG_EINVAL).  The
  * kernels' bookkeeping and per-particle working state live in a static device
  * array of FJG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds
  * until exit.  The first call on each device looks up that array's address; make it
@@ -153,7 +153,7 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
  * on the GPU race and must be serialised by the caller. */
 #define FJG_NOALLOC_MAX_EVENTS 65536
 #define FJG_NOALLOC_MAX_PARTICLES 131072
-#define FJG_NOALLOC_SCRATCH_BYTES (7 * 8 * FJG_NOALLOC_MAX_PARTICLES + (1 << 20) + 16384)
+#define FJG_NOALLOC_SCRATCH_BYTES ((7 * 8 + 96) * FJG_NOALLOC_MAX_PARTICLES + 5 * 4 * FJG_NOALLOC_MAX_EVENTS + 16384)
 fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t* offsets, int n_events, int64_t total,
                                      const int32_t* algo, int algo_all, const double* radius, double r_all,
                                      const fjg_outputs* out, void* stream);

@@ -160,9 +160,18 @@ def test_pseudojet_records_in_place(ctx):
 
 
 def test_too_big_is_reported(ctx):
+    """Events above the largest supported size (2**24 particles) are refused
+    on the host before anything is read or launched."""
+    import ctypes
+    import torch
     import fastjet_gpu_gb300 as F
-    ev = E.single_event(3000, 2, seed=1)
-    with pytest.raises(F.FjgError) as ei:
-        ctx.cluster_batch(ev, np.array([0, 3000]), -1, 0.4)
-    assert ei.value.status == 4
-    ctx.cluster_batch(ev[:100], np.array([0, 100]), -1, 0.4)  # the context stays usable
+    small = torch.zeros((8, 4), dtype=torch.float64, device="cuda")
+    jets = torch.zeros((8, 4), dtype=torch.float64, device="cuda")
+    lab = torch.zeros(8, dtype=torch.int32, device="cuda")
+    nj = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = F.lib().fjg_cluster_event(ctx._h, ctypes.c_void_p(small.data_ptr()), (1 << 24) + 1, -1, 0.4,
+                                   ctypes.c_void_p(jets.data_ptr()), ctypes.c_void_p(lab.data_ptr()),
+                                   ctypes.c_void_p(nj.data_ptr()), None, None)
+    assert st == 4
+    ev = E.single_event(100, 2, seed=1)
+    ctx.cluster_batch(ev, np.array([0, 100]), -1, 0.4)  # the context stays usable
