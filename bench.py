@@ -1,10 +1,13 @@
 """Benchmark: batched jet clustering on one GB300 (events/s).
 
-Workload (one "step"): 4096 events, particle counts log-uniform in [50, 2000]
-(seeded generator, Poisson(3)+1 hard axes), anti-kt R=0.4 in FP64, clustered in
-one batched call (one persistent kernel per size bucket).
+Default workload (one "step"): 4096 events, particle counts log-uniform in
+[50, 2000] (seeded generator, Poisson(3)+1 hard axes), anti-kt R=0.4 in FP64,
+clustered in one batched call (one persistent kernel per size bucket).
+``--workload pileup``: 64 pile-up-like events of 10k-60k particles (soft pT
+Exp(0.6 GeV), eta U[-4, 4], 2-6 hard axes), anti-kt R=0.4, with kt R=0.6
+reported beside it (the tiled kernel).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload mixed|pileup]
 
 Prints one JSON line.  ``value`` is events/s with the inputs resident in HBM,
 timed with CUDA events on the library's stream around each step, L2 flushed
@@ -32,12 +35,24 @@ sys.path.insert(0, ROOT)
 
 from fastjet_gpu_gb300 import events as E  # noqa: E402
 
-N_EVENTS = 4096
-N_LO, N_HI = 50, 2000
 ALGO, RADIUS = -1, 0.4
-SEED = 3
-METRIC = "events/s, batched anti-kt R=0.4 clustering of 4096 events (50-2000 particles)"
-WORKLOAD = "4096 events, particle counts log-uniform in [50, 2000], anti-kt R=0.4, FP64, one batched call"
+WORKLOADS = {
+    "mixed": dict(
+        events=4096, make=lambda n: E.mixed_batch(n, 50, 2000, seed=3), flush=True, cpu_start=64,
+        per_event_sample=256, second=None,
+        metric="events/s, batched anti-kt R=0.4 clustering of 4096 events (50-2000 particles)",
+        workload="4096 events, particle counts log-uniform in [50, 2000], anti-kt R=0.4, FP64, one batched call"),
+    "pileup": dict(
+        events=64, make=lambda n: E.pileup_batch(n, 10000, 60000, seed=4), flush=False, cpu_start=16,
+        per_event_sample=4, second=(1, 0.6),
+        metric="events/s, batched anti-kt R=0.4 clustering of 64 pile-up events (10k-60k particles)",
+        workload="64 pile-up-like events, 10k-60k particles, anti-kt R=0.4 (kt R=0.6 beside it), FP64, "
+                 "one batched call"),
+}
+W = WORKLOADS["mixed"]
+N_EVENTS = W["events"]
+METRIC = W["metric"]
+WORKLOAD = W["workload"]
 
 
 def _peaks():
@@ -102,14 +117,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_cluster_rate(batch, threads, target_s=10.0, max_events=None):
+def cpu_cluster_rate(batch, threads, target_s=10.0, max_events=None, algo=None, radius=None):
     """Oracle events/s on `threads` host threads over a bounded prefix sample."""
     import oracle
-    n = min(64, batch.n_events)
+    algo = ALGO if algo is None else algo
+    radius = RADIUS if radius is None else radius
+    n = min(W["cpu_start"], batch.n_events)
     while True:
         off = batch.offsets[: n + 1]
         t0 = time.perf_counter()
-        oracle.cluster_batch(batch.particles[: off[-1]], off, ALGO, RADIUS, threads=threads, want_history=False)
+        oracle.cluster_batch(batch.particles[: off[-1]], off, algo, radius, threads=threads, want_history=False)
         dt = time.perf_counter() - t0
         if dt >= target_s or n >= batch.n_events or (max_events and n >= max_events):
             return n / dt, n, dt
@@ -119,7 +136,7 @@ def cpu_cluster_rate(batch, threads, target_s=10.0, max_events=None):
 def run_reference(args, rank):
     if rank != 0:
         return
-    batch = E.mixed_batch(N_EVENTS, N_LO, N_HI, seed=SEED)
+    batch = W["make"](N_EVENTS)
     cores = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_cluster_rate(batch, cores, target_s=0.5)
@@ -152,7 +169,7 @@ def run_ours(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    batch = E.mixed_batch(N_EVENTS, N_LO, N_HI, seed=SEED)
+    batch = W["make"](N_EVENTS)
     total = int(batch.offsets[-1])
     ctx = F.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
@@ -164,37 +181,41 @@ def run_ours(args, rank, world, local_rank):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
 
-    def step():
-        ctx.cluster_batch_device(p4, off, ALGO, RADIUS, total=total, out=out)
+    def step(algo=ALGO, radius=RADIUS):
+        ctx.cluster_batch_device(p4, off, algo, radius, total=total, out=out)
 
     for _ in range(max(args.warmup, 3)):
         step()
     ctx.check()
     n_jets_total = int(out["n_jets"].sum().item())
 
+    def timed_steps(k_steps, algo=ALGO, radius=RADIUS):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(k_steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(k_steps)]
+        for k in range(k_steps):
+            with torch.cuda.stream(stream):
+                if W["flush"]:
+                    flush.fill_(float(k))  # evict L2 between steps (inputs are ~70 MB < 129 MB L2)
+                starts[k].record(stream)
+            step(algo, radius)
+            with torch.cuda.stream(stream):
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+        return [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
+
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local_rank) as clk:
         t_wall = time.perf_counter()
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(float(k))  # evict L2 between steps (inputs are ~70 MB < 129 MB L2)
-                starts[k].record(stream)
-            step()
-            with torch.cuda.stream(stream):
-                ends[k].record(stream)
-        torch.cuda.synchronize()
+        step_ms = timed_steps(args.steps)
         t_wall = time.perf_counter() - t_wall
     ctx.check()
     barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     dev_s = sum(step_ms) / 1e3
     if world > 1:
         import torch.distributed as dist
@@ -221,6 +242,33 @@ def run_ours(args, rank, world, local_rank):
         e2e_s = float(t.item())
     assert int(res["n_jets"].sum()) == n_jets_total
     h2d = batch.particles.nbytes + batch.offsets.nbytes
+
+    # the plain path: one event per launch, synchronous (the per-event-launch
+    # comparator), on an evenly spaced sample of the same events
+    idx = np.linspace(0, N_EVENTS - 1, min(W["per_event_sample"], N_EVENTS)).astype(int)
+    sample = [torch.from_numpy(batch.event(int(e))).to(dev) for e in idx]
+    ctx.cluster_event(sample[0], ALGO, RADIUS)
+    lat = []
+    for ev in sample:
+        t0 = time.perf_counter()
+        ctx.cluster_event(ev, ALGO, RADIUS)
+        lat.append(time.perf_counter() - t0)
+    sizes = batch.sizes()
+    # event sizes are drawn independently of their position, so an evenly
+    # spaced sample follows the batch's size distribution
+    per_event = {"value": len(lat) / sum(lat) if sum(lat) > 0 else None, "unit": "events/s",
+                 "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                 "sample": f"{len(lat)} events evenly spaced in the batch (sizes {int(sizes[idx].min())}-"
+                           f"{int(sizes[idx].max())}), fjg_cluster_event, synchronous, device inputs"}
+    second = None
+    if W["second"] is not None:
+        a2, r2 = W["second"]
+        step(a2, r2)
+        ctx.check()
+        ms2 = timed_steps(max(1, min(args.steps, 3)), a2, r2)
+        second = {"algorithm": {1: "kt", 0: "cambridge-aachen", -1: "anti-kt"}[a2], "R": r2,
+                  "value": N_EVENTS * len(ms2) / (sum(ms2) / 1e3), "unit": "events/s",
+                  "ms_per_step": float(np.mean(ms2))}
     d2h = total * 32 + total * 4 + N_EVENTS * 4
 
     # roofline of the clustering kernels: algorithmic HBM bytes per step
@@ -237,22 +285,27 @@ def run_ours(args, rank, world, local_rank):
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * step_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "events": N_EVENTS, "particles": total, "algorithm": "anti-kt",
-                       "R": RADIUS, "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{world}"},
+                       "R": RADIUS, "l2": ("flushed between steps (256 MiB write)" if W["flush"] else
+                                           "not flushed: a step runs for a second or more"),
+                       "parallelism": f"replicas{world}"},
+            "per_event_launch": per_event,
             "e2e": {"value": world * N_EVENTS / e2e_s, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"peak {peak_kind}; the kernels are latency-bound (sequential merge steps), "
                                  f"HBM carries only staging ({alg_bytes} B per step)"},
-            "gpu_launches": args.steps * (1 + 4),
+            "gpu_launches": args.steps * 9,  # 4 bucketing kernels, the tiled kernel, 4 bucket kernels
             "clocks": clk.summary(),
             "wall_s": t_wall}
+    if second is not None:
+        line["config"]["second"] = second
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         v, n, dt = cpu_cluster_rate(batch, cores, target_s=10.0)
         line["cpu_baseline"] = {"value": v, "unit": "events/s", "cores": cores, "kind": "port",
-                                "sample": f"first {n} of the 4096 events ({dt:.1f} s), oracle nearest-neighbour "
-                                          f"clustering, one event per thread"}
+                                "sample": f"first {n} of the {N_EVENTS} events ({dt:.1f} s), oracle "
+                                          f"nearest-neighbour clustering, one event per thread"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -265,10 +318,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--events", type=int, default=N_EVENTS,
-                    help="events per step (default 4096; smaller only for profiling captures)")
+    ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS))
+    ap.add_argument("--events", type=int, default=None,
+                    help="events per step (default: the workload's; smaller only for profiling captures)")
     args = ap.parse_args()
-    globals()["N_EVENTS"] = args.events
+    w = WORKLOADS[args.workload]
+    globals().update(W=w, N_EVENTS=args.events or w["events"], METRIC=w["metric"], WORKLOAD=w["workload"])
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
