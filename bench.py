@@ -11,7 +11,9 @@ reported beside it (the tiled kernel).
 
 Prints one JSON line.  ``value`` is events/s with the inputs resident in HBM,
 timed with CUDA events on the library's stream around each step, L2 flushed
-(256 MiB write) between steps.  ``e2e`` is the same metric through the
+(256 MiB write) between steps; each step is one launch of a CUDA graph that
+holds the batch call, after the autotuner has picked the launch configuration
+(``--no-graph`` / ``--no-tune`` turn either off).  ``e2e`` is the same metric through the
 host-memory entry point (pinned host buffers; H2D copy of the inputs, the
 kernels, D2H copy of the outputs and a synchronisation inside each step).
 ``--impl reference`` times the CPU clustering that stands in for the
@@ -180,13 +182,27 @@ def run_ours(args, rank, world, local_rank):
            "n_jets": torch.empty(N_EVENTS, dtype=torch.int32, device=dev)}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
+    tuning = None
+    if not args.no_tune:
+        # per-bucket kernel shape and CTAs per SM (and the tile side when the
+        # workload has events above 2048 particles), timed on synthetic events
+        tuning = ctx.autotune(ALGO, RADIUS, skip_large=int(batch.sizes().max()) <= 2048)
+    graph = None if args.no_graph else ctx.capture_batch(p4, off, ALGO, RADIUS, total=total, out=out)
 
     def step(algo=ALGO, radius=RADIUS):
-        ctx.cluster_batch_device(p4, off, algo, radius, total=total, out=out)
+        if graph is not None and (algo, radius) == (ALGO, RADIUS):
+            graph.launch()
+        else:
+            ctx.cluster_batch_device(p4, off, algo, radius, total=total, out=out)
+
+    def check():
+        ctx.check()
+        if graph is not None:
+            graph.check()
 
     for _ in range(max(args.warmup, 3)):
         step()
-    ctx.check()
+    check()
     n_jets_total = int(out["n_jets"].sum().item())
 
     def timed_steps(k_steps, algo=ALGO, radius=RADIUS):
@@ -214,7 +230,7 @@ def run_ours(args, rank, world, local_rank):
         t_wall = time.perf_counter()
         step_ms = timed_steps(args.steps)
         t_wall = time.perf_counter() - t_wall
-    ctx.check()
+    check()
     barrier()
     dev_s = sum(step_ms) / 1e3
     if world > 1:
@@ -287,7 +303,8 @@ def run_ours(args, rank, world, local_rank):
             "config": {"workload": WORKLOAD, "events": N_EVENTS, "particles": total, "algorithm": "anti-kt",
                        "R": RADIUS, "l2": ("flushed between steps (256 MiB write)" if W["flush"] else
                                            "not flushed: a step runs for a second or more"),
-                       "parallelism": f"replicas{world}"},
+                       "parallelism": f"replicas{world}", "cuda_graph": graph is not None,
+                       "tuning": tuning},
             "per_event_launch": per_event,
             "e2e": {"value": world * N_EVENTS / e2e_s, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
@@ -308,6 +325,8 @@ def run_ours(args, rank, world, local_rank):
                                           f"nearest-neighbour clustering, one event per thread"}
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if graph is not None:
+        graph.close()
     ctx.close()
 
 
@@ -318,6 +337,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--no-graph", action="store_true", help="launch through the API instead of a CUDA graph")
     ap.add_argument("--workload", default="mixed", choices=sorted(WORKLOADS))
     ap.add_argument("--events", type=int, default=None,
                     help="events per step (default: the workload's; smaller only for profiling captures)")

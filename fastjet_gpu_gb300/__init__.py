@@ -53,6 +53,29 @@ class _Outputs(ctypes.Structure):
                 ("history", ctypes.c_void_p), ("owner", ctypes.c_void_p)]
 
 
+class _Tuning(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32 * 5), ("slots_per_thread", ctypes.c_int32 * 5),
+                ("ctas_per_sm", ctypes.c_int32 * 5), ("events_per_s", ctypes.c_double * 5),
+                ("large_ctas_per_sm", ctypes.c_int32), ("tile_factor", ctypes.c_double)]
+
+    def to_dict(self):
+        return {"threads": list(self.threads), "slots_per_thread": list(self.slots_per_thread),
+                "ctas_per_sm": list(self.ctas_per_sm), "events_per_s": list(self.events_per_s),
+                "large_ctas_per_sm": self.large_ctas_per_sm, "tile_factor": self.tile_factor}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        for k in ("threads", "slots_per_thread", "ctas_per_sm"):
+            getattr(t, k)[:] = [int(x) for x in d[k]]
+        t.events_per_s[:] = [float(x) for x in d.get("events_per_s", [0.0] * 5)]
+        t.large_ctas_per_sm = int(d["large_ctas_per_sm"])
+        t.tile_factor = float(d["tile_factor"])
+        return t
+
+
+FJG_TUNE_SKIP_LARGE = 1
+
 _lib = None
 
 
@@ -79,6 +102,15 @@ def lib():
         L.fjg_cluster_event.argtypes = [P, P, I, I, D, P, P, P, P, P]
         L.fjg_cluster_pseudojets.argtypes = [P, P, I, I, D, P]
         L.fjg_kinematics.argtypes = [P, P, I, I, P, P, P, P]
+        L.fjg_graph_capture_batch.argtypes = [P, P, P, I, ctypes.c_int64, P, I, P, D, ctypes.POINTER(_Outputs),
+                                              ctypes.POINTER(P)]
+        L.fjg_graph_launch.argtypes = [P, P]
+        L.fjg_graph_check.argtypes = [P]
+        L.fjg_graph_destroy.argtypes = [P]
+        L.fjg_graph_destroy.restype = None
+        L.fjg_get_tuning.argtypes = [P, ctypes.POINTER(_Tuning)]
+        L.fjg_set_tuning.argtypes = [P, ctypes.POINTER(_Tuning)]
+        L.fjg_autotune.argtypes = [P, I, D, I, ctypes.POINTER(_Tuning)]
         _lib = L
     return _lib
 
@@ -193,6 +225,54 @@ class Context:
         self._check(st)
         return out
 
+    def capture_batch(self, p4, offsets, algo, radius, total=None, history=False, owner=False, out=None):
+        """Capture one batch call on these device tensors as a CUDA graph.
+
+        Returns a ``Graph``; refill the tensors in place (event sizes may
+        change as long as the last offset stays <= total) and launch again.
+        """
+        import torch
+        ne = offsets.numel() - 1
+        total = p4.shape[0] if total is None else total
+        if out is None:
+            dev = p4.device
+            out = {"jets": torch.empty((max(total, 1), 4), dtype=torch.float64, device=dev),
+                   "jet_label": torch.empty(max(total, 1), dtype=torch.int32, device=dev),
+                   "n_jets": torch.empty(max(ne, 1), dtype=torch.int32, device=dev)}
+            if history:
+                out["history"] = torch.empty((max(total, 1), 2), dtype=torch.float64, device=dev)
+            if owner:
+                out["owner"] = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+        o = _Outputs(out["jets"].data_ptr(), out["jet_label"].data_ptr(), out["n_jets"].data_ptr(),
+                     out["history"].data_ptr() if "history" in out else None,
+                     out["owner"].data_ptr() if "owner" in out else None)
+        a_t = None if isinstance(algo, (int, np.integer)) else algo
+        r_t = None if isinstance(radius, (float, int, np.floating)) else radius
+        h = ctypes.c_void_p()
+        st = lib().fjg_graph_capture_batch(self._h, _t_ptr(p4), _t_ptr(offsets), ne, int(total), _t_ptr(a_t),
+                                           int(algo) if a_t is None else 0, _t_ptr(r_t),
+                                           float(radius) if r_t is None else 0.0, ctypes.byref(o), ctypes.byref(h))
+        self._check(st)
+        return Graph(self, h, out, (p4, offsets, a_t, r_t))
+
+    @property
+    def tuning(self):
+        t = _Tuning()
+        self._check(lib().fjg_get_tuning(self._h, ctypes.byref(t)))
+        return t.to_dict()
+
+    @tuning.setter
+    def tuning(self, d):
+        t = _Tuning.from_dict(d)
+        self._check(lib().fjg_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, algo=-1, radius=0.4, skip_large=False):
+        """Time the compiled kernel shapes per size bucket; keep and return the fastest."""
+        t = _Tuning()
+        self._check(lib().fjg_autotune(self._h, int(algo), float(radius), FJG_TUNE_SKIP_LARGE if skip_large else 0,
+                                       ctypes.byref(t)))
+        return t.to_dict()
+
     def cluster_event(self, p4, algo, radius, history=False, owner=False):
         """The plain path: one event per launch (torch CUDA tensors), synchronous."""
         import torch
@@ -239,6 +319,30 @@ class Context:
         if host is not None:
             host.view(np.uint8).reshape(-1)[:] = dev.cpu().numpy()
         return records
+
+
+class Graph:
+    """A captured batch call (fjg_graph_*): ``launch()`` reruns it on the captured tensors."""
+
+    def __init__(self, ctx, handle, out, keep):
+        self.ctx, self._h, self.out, self._keep = ctx, handle, out, keep
+
+    def launch(self, stream=None):
+        self.ctx._check(lib().fjg_graph_launch(self._h, ctypes.c_void_p(stream) if stream else None))
+
+    def check(self):
+        self.ctx._check(lib().fjg_graph_check(self._h))
+
+    def close(self):
+        if self._h:
+            lib().fjg_graph_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _default_ctx = {}

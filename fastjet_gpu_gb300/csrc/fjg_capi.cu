@@ -8,58 +8,17 @@
 #include <cuda_runtime.h>
 
 #include "fastjet_gb300.h"
-#include "fjg_kernels.cuh"
+#include "fjg_context.h"
 
 using fjg::BatchArgs;
 
 namespace {
-
 thread_local std::string g_thread_error;
-
-struct DeviceBuffer {
-  void* ptr = nullptr;
-  size_t cap = 0;
-  cudaError_t reserve(size_t bytes) {
-    if (bytes <= cap) return cudaSuccess;
-    if (ptr) {
-      cudaDeviceSynchronize();  // the old buffer may still be in use by queued work
-      cudaFree(ptr);
-    }
-    ptr = nullptr;
-    cap = 0;
-    size_t want = bytes + bytes / 4 + 256;
-    cudaError_t err = cudaMalloc(&ptr, want);
-    if (err == cudaSuccess) cap = want;
-    return err;
-  }
-  void release() {
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-  }
-};
-
 }  // namespace
 
 void fjg::set_thread_error(const char* msg) { g_thread_error = msg; }
 
-struct fjg_ctx {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  cudaStream_t side[fjg::kNumQueues] = {};
-  cudaEvent_t ev_fork = nullptr;
-  cudaEvent_t ev_join[fjg::kNumQueues] = {};
-  fjg::Scratch sc{};
-  DeviceBuffer scratch;  // order/counts/queues/status/offsets1
-  DeviceBuffer io;       // device copies for the host-memory entry points
-  DeviceBuffer single;   // outputs of fjg_cluster_pseudojets
-  DeviceBuffer wsbuf;    // exact per-particle state of the clustering kernels
-  DeviceBuffer largebuf; // state of the tiled kernel (events above 2048 particles)
-  std::string last_error;
-};
-
-namespace {
+namespace fjg {
 
 fjg_status set_error(fjg_ctx* ctx, fjg_status st, const std::string& msg) {
   if (ctx)
@@ -74,83 +33,78 @@ fjg_status cuda_error(fjg_ctx* ctx, cudaError_t err, const char* what) {
   return set_error(ctx, err == cudaErrorMemoryAllocation ? FJG_ENOMEM : FJG_ECUDA, m);
 }
 
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    cudaGetDevice(&prev);
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    cudaGetDevice(&cur);
-    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-  }
-};
-
-// Ensure the device scratch can describe `n_events` events.
-cudaError_t ensure_scratch(fjg_ctx* ctx, int n_events) {
-  if (n_events < 1) n_events = 1;
-  if (ctx->sc.order && ctx->sc.cap_events >= n_events) return cudaSuccess;
-  int cap = n_events + n_events / 4 + 64;
-  const size_t hist_bytes = (sizeof(int32_t) * fjg::kHistBins + 255) & ~size_t(255);
-  size_t bytes = sizeof(int32_t) * (size_t)fjg::kNumQueues * cap + 256 + hist_bytes;
-  cudaError_t err = ctx->scratch.reserve(bytes);
-  if (err != cudaSuccess) return err;
-  char* p = static_cast<char*>(ctx->scratch.ptr);
-  ctx->sc.offsets1 = reinterpret_cast<int64_t*>(p);
-  ctx->sc.counts = reinterpret_cast<int32_t*>(p + 64);
-  ctx->sc.queues = reinterpret_cast<int*>(p + 128);
-  ctx->sc.status = reinterpret_cast<int*>(p + 192);
-  ctx->sc.hist = reinterpret_cast<int32_t*>(p + 256);
-  ctx->sc.order = reinterpret_cast<int32_t*>(p + 256 + hist_bytes);
-  ctx->sc.cap_events = cap;
-  err = cudaMemset(ctx->sc.status, 0, sizeof(int));
-  if (err == cudaSuccess) err = cudaDeviceSynchronize();
-  return err;
-}
-
-// Ensure the kernels' per-particle workspace holds `particles` entries.
-cudaError_t ensure_ws(fjg_ctx* ctx, int64_t particles) {
-  if (particles < 1) particles = 1;
-  if (ctx->sc.ws && ctx->sc.ws_stride >= particles) return cudaSuccess;
-  const int64_t stride = particles + particles / 4 + 1024;
-  cudaError_t err = ctx->wsbuf.reserve(sizeof(double) * fjg::kWsFields * (size_t)stride);
-  if (err != cudaSuccess) return err;
-  ctx->sc.ws = static_cast<double*>(ctx->wsbuf.ptr);
-  ctx->sc.ws_stride = (int64_t)(ctx->wsbuf.cap / (sizeof(double) * fjg::kWsFields));
-  return cudaSuccess;
-}
-
-// Ensure the tiled kernel's workspace covers `particles` entries (batches
-// whose particles all fit the shared-memory path need none).
-cudaError_t ensure_large_ws(fjg_ctx* ctx, int64_t particles) {
-  if (particles <= fjg::kSmemMaxN) return cudaSuccess;
-  if (ctx->sc.large_ws && ctx->sc.large_ws_particles >= particles) return cudaSuccess;
-  cudaError_t err = ctx->largebuf.reserve((size_t)fjg::kLargeWsBytesPerParticle * (size_t)particles + 256);
-  if (err != cudaSuccess) return err;
-  ctx->sc.large_ws = static_cast<unsigned char*>(ctx->largebuf.ptr);
-  ctx->sc.large_ws_particles = (int64_t)((ctx->largebuf.cap - 256) / fjg::kLargeWsBytesPerParticle);
-  return cudaSuccess;
+fjg_status status_to_error(fjg_ctx* ctx, int st) {
+  if (!st) return FJG_OK;
+  if (st & kStatusTooBig) return set_error(ctx, FJG_ETOOBIG, "an event exceeds the supported particle count");
+  if (st & kStatusInternal)
+    return set_error(ctx, FJG_EKERNEL, "a clustering kernel found no candidate (non-finite input?)");
+  return set_error(ctx, FJG_EINVAL, "invalid event offsets");
 }
 
 bool valid_algo(int a) { return a == FJG_KT || a == FJG_CAM || a == FJG_ANTIKT; }
 
+cudaError_t ScratchSet::reserve_lists(int n_events) {
+  if (n_events < 1) n_events = 1;
+  if (sc.order && sc.cap_events >= n_events) return cudaSuccess;
+  int cap = n_events + n_events / 4 + 64;
+  const size_t hist_bytes = (sizeof(int32_t) * kHistBins + 255) & ~size_t(255);
+  size_t bytes = sizeof(int32_t) * (size_t)kNumQueues * cap + 256 + hist_bytes;
+  cudaError_t err = lists.reserve(bytes);
+  if (err != cudaSuccess) return err;
+  char* p = static_cast<char*>(lists.ptr);
+  sc.offsets1 = reinterpret_cast<int64_t*>(p);
+  sc.counts = reinterpret_cast<int32_t*>(p + 64);
+  sc.queues = reinterpret_cast<int*>(p + 128);
+  sc.status = reinterpret_cast<int*>(p + 192);
+  sc.hist = reinterpret_cast<int32_t*>(p + 256);
+  sc.order = reinterpret_cast<int32_t*>(p + 256 + hist_bytes);
+  sc.cap_events = cap;
+  err = cudaMemset(sc.status, 0, sizeof(int));
+  if (err == cudaSuccess) err = cudaDeviceSynchronize();
+  return err;
+}
+
+cudaError_t ScratchSet::reserve_ws(int64_t particles) {
+  if (particles < 1) particles = 1;
+  if (sc.ws && sc.ws_stride >= particles) return cudaSuccess;
+  const int64_t stride = particles + particles / 4 + 1024;
+  cudaError_t err = ws.reserve(sizeof(double) * kWsFields * (size_t)stride);
+  if (err != cudaSuccess) return err;
+  sc.ws = static_cast<double*>(ws.ptr);
+  sc.ws_stride = (int64_t)(ws.cap / (sizeof(double) * kWsFields));
+  return cudaSuccess;
+}
+
+cudaError_t ScratchSet::reserve_large(int64_t particles) {
+  if (particles <= kSmemMaxN) return cudaSuccess;
+  if (sc.large_ws && sc.large_ws_particles >= particles) return cudaSuccess;
+  cudaError_t err = large.reserve((size_t)kLargeWsBytesPerParticle * (size_t)particles + 256);
+  if (err != cudaSuccess) return err;
+  sc.large_ws = static_cast<unsigned char*>(large.ptr);
+  sc.large_ws_particles = (int64_t)((large.cap - 256) / kLargeWsBytesPerParticle);
+  return cudaSuccess;
+}
+
+}  // namespace fjg
+
+using fjg::cuda_error;
+using fjg::DeviceGuard;
+using fjg::set_error;
+using fjg::valid_algo;
+
+namespace {
+
 // Read and clear the kernels' status word (synchronises the stream).
 fjg_status take_status(fjg_ctx* ctx, cudaStream_t s) {
   int st = 0;
-  cudaError_t err = cudaMemcpyAsync(&st, ctx->sc.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaError_t err = cudaMemcpyAsync(&st, ctx->scratch.sc.status, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);
   if (err != cudaSuccess) return cuda_error(ctx, err, "clustering");
   if (st) {
-    cudaMemsetAsync(ctx->sc.status, 0, sizeof(int), s);
+    cudaMemsetAsync(ctx->scratch.sc.status, 0, sizeof(int), s);
     cudaStreamSynchronize(s);
-    if (st & fjg::kStatusTooBig)
-      return set_error(ctx, FJG_ETOOBIG, "an event exceeds the supported particle count");
-    if (st & fjg::kStatusInternal)
-      return set_error(ctx, FJG_EKERNEL, "a clustering kernel found no candidate (non-finite input?)");
-    return set_error(ctx, FJG_EINVAL, "invalid event offsets");
   }
-  return FJG_OK;
+  return fjg::status_to_error(ctx, st);
 }
 
 }  // namespace
@@ -191,7 +145,7 @@ fjg_status fjg_ctx_create(int device, fjg_ctx** out) {
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ctx->ev_join[b], cudaEventDisableTiming);
   }
   if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
-  if (err == cudaSuccess) err = ensure_scratch(ctx, 1024);
+  if (err == cudaSuccess) err = ctx->scratch.reserve_lists(1024);
   if (err != cudaSuccess) {
     fjg_status st = cuda_error(nullptr, err, "context creation");
     fjg_ctx_destroy(ctx);
@@ -217,8 +171,6 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
   ctx->scratch.release();
   ctx->io.release();
   ctx->single.release();
-  ctx->wsbuf.release();
-  ctx->largebuf.release();
   delete ctx;
 }
 
@@ -241,9 +193,9 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   if (!algo && !valid_algo(algo_all)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
   if (!radius && !(r_all > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
   DeviceGuard g(ctx->device);
-  cudaError_t err = ensure_scratch(ctx, n_events);
-  if (err == cudaSuccess) err = ensure_ws(ctx, total);
-  if (err == cudaSuccess) err = ensure_large_ws(ctx, total);
+  cudaError_t err = ctx->scratch.reserve_lists(n_events);
+  if (err == cudaSuccess) err = ctx->scratch.reserve_ws(total);
+  if (err == cudaSuccess) err = ctx->scratch.reserve_large(total);
   if (err != cudaSuccess) return cuda_error(ctx, err, "scratch allocation");
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   BatchArgs A{};
@@ -259,8 +211,9 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   A.n_jets = out->n_jets;
   A.history = reinterpret_cast<fjg::StepRec*>(out->history);
   A.owner = out->owner;
-  A.status = ctx->sc.status;
-  err = fjg::launch_batch(A, ctx->sc, n_events, ctx->num_sms, s, ctx->side, &ctx->ev_fork, ctx->ev_join);
+  A.status = ctx->scratch.sc.status;
+  err = fjg::launch_batch(A, ctx->scratch.sc, n_events, ctx->num_sms, ctx->tune, s, ctx->side, &ctx->ev_fork,
+                          ctx->ev_join);
   if (err != cudaSuccess) return cuda_error(ctx, err, "batch launch");
   return FJG_OK;
 }
@@ -339,8 +292,8 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
     return err == cudaSuccess ? FJG_OK : cuda_error(ctx, err, "fjg_cluster_event");
   }
   if (n > fjg::kLargeMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the supported particle count");
-  cudaError_t werr = ensure_ws(ctx, n);
-  if (werr == cudaSuccess) werr = ensure_large_ws(ctx, n);
+  cudaError_t werr = ctx->scratch.reserve_ws(n);
+  if (werr == cudaSuccess) werr = ctx->scratch.reserve_large(n);
   if (werr != cudaSuccess) return cuda_error(ctx, werr, "workspace allocation");
   BatchArgs A{};
   A.p4 = p4;
@@ -354,8 +307,8 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
   A.n_jets = n_jets;
   A.history = reinterpret_cast<fjg::StepRec*>(history);
   A.owner = owner;
-  A.status = ctx->sc.status;
-  cudaError_t err = fjg::launch_single(A, ctx->sc, n, s);
+  A.status = ctx->scratch.sc.status;
+  cudaError_t err = fjg::launch_single(A, ctx->scratch.sc, n, ctx->tune, s);
   if (err != cudaSuccess) return cuda_error(ctx, err, "fjg_cluster_event launch");
   return take_status(ctx, s);
 }
@@ -384,8 +337,8 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t b_jets = al(sizeof(double) * 4 * size), b_lab = al(sizeof(int32_t) * size);
   cudaError_t err = ctx->single.reserve(b_jets + b_lab + 256);
-  if (err == cudaSuccess) err = ensure_ws(ctx, size);
-  if (err == cudaSuccess) err = ensure_large_ws(ctx, size);
+  if (err == cudaSuccess) err = ctx->scratch.reserve_ws(size);
+  if (err == cudaSuccess) err = ctx->scratch.reserve_large(size);
   if (err != cudaSuccess) return cuda_error(ctx, err, "device buffers");
   char* d = static_cast<char*>(ctx->single.ptr);
   double* jets = reinterpret_cast<double*>(d);
@@ -400,8 +353,8 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
   A.jets = jets;
   A.jet_label = labels;
   A.n_jets = nj;
-  A.status = ctx->sc.status;
-  err = fjg::launch_single(A, ctx->sc, size, s);
+  A.status = ctx->scratch.sc.status;
+  err = fjg::launch_single(A, ctx->scratch.sc, size, ctx->tune, s);
   if (err == cudaSuccess) err = fjg::launch_pseudojet_epilogue(particles, size, jets, labels, nj, s);
   if (err != cudaSuccess) return cuda_error(ctx, err, "fjg_cluster_pseudojets");
   return take_status(ctx, s);

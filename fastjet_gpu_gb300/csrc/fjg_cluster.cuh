@@ -69,6 +69,7 @@ struct BatchArgs {
   int32_t* owner;          // [total] or null
   int* status;             // device error flag (0 = ok)
   unsigned char* large_ws; // tiled-path workspace: event e at large_ws + 96 * offsets[e] (null: none)
+  double tile_factor;      // tiled path: tile side >= tile_factor * R (>= 1)
 };
 
 constexpr int kRescanChunk = 8;  // targets per register pass

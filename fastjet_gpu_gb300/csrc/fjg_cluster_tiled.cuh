@@ -1,4 +1,4 @@
-// Clustering of large events (more than 2048 particles): one CTA per event,
+// Clustering of large events (more than 4096 particles): one CTA per event,
 // state in a global workspace, nearest neighbours restricted to a 3x3 window
 // of rapidity-azimuth tiles.  (The reference's grid backend, grid.cu:55-549,
 // also tiles the plane with cells of side >= R and compares adjacent cells;
@@ -474,7 +474,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     lo = fmax(lo, -15.0);
     hi = fmin(hi, 15.0);
     if (!(hi >= lo)) hi = lo;
-    const double side_min = R * (1.0 + 1e-4) + 1e-5;
+    const double side_min = R * fmax(A.tile_factor, 1.0) * (1.0 + 1e-4) + 1e-5;
     int nphi = (int)fmin(floor(6.283185307179586 / side_min), 4096.0);
     nphi = nphi < 1 ? 1 : nphi;
     int nrap = (int)fmin(floor((hi - lo) / side_min), 4096.0);

@@ -1,24 +1,8 @@
 // Persistent clustering kernels (one per size bucket) and the bucketing pass.
 #include "fjg_kernels.cuh"
+#include "fjg_variants.cuh"
 
 namespace fjg {
-
-template <int T, int SPT>
-__global__ void __launch_bounds__(T) k_cluster_smem(BatchArgs A) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemLayout<T, SPT>& S = *reinterpret_cast<SmemLayout<T, SPT>*>(smem_raw);
-  const int count = *A.n_order;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const int q = atomicAdd(A.queue, 1);
-      S.event = (q < count) ? A.order[q] : -1;
-    }
-    __syncthreads();
-    const int e = S.event;
-    if (e < 0) break;
-    cluster_event_smem<T, SPT>(S, A, e);  // ends with a barrier
-  }
-}
 
 // Persistent tiled kernel for events above kSmemMaxN particles.
 __global__ void __launch_bounds__(kTiledT) k_cluster_tiled(BatchArgs A) {
@@ -91,13 +75,21 @@ __global__ void __launch_bounds__(1024) k_large_sort(const int64_t* offsets, int
 // One block of 1024 threads: hist[n] becomes the position of the first event
 // of size n inside its bucket's list (sizes in descending order), counts[b]
 // the number of events of bucket b.
+constexpr int kScanPerThread = kSmemMaxN / 1024;
+
 __global__ void __launch_bounds__(1024) k_size_scan(int32_t* hist, int32_t* counts) {
   __shared__ int32_t warp_sum[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // thread tid owns sizes n = kSmemMaxN - 2 tid and kSmemMaxN - 2 tid - 1 (descending)
-  const int n0 = kSmemMaxN - 2 * tid, n1 = n0 - 1;
-  const int h0 = hist[n0], h1 = (n1 >= 1) ? hist[n1] : 0;
-  int incl = h0 + h1;
+  // thread tid owns sizes n = kSmemMaxN - kScanPerThread * tid - k (descending)
+  const int n_first = kSmemMaxN - kScanPerThread * tid;
+  int h[kScanPerThread];
+  int mine = 0;
+  for (int k = 0; k < kScanPerThread; ++k) {
+    const int n = n_first - k;
+    h[k] = (n >= 1) ? hist[n] : 0;
+    mine += h[k];
+  }
+  int incl = mine;
   for (int o = 1; o < 32; o <<= 1) {
     const int v = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += v;
@@ -113,19 +105,23 @@ __global__ void __launch_bounds__(1024) k_size_scan(int32_t* hist, int32_t* coun
     warp_sum[lane] = v;
   }
   __syncthreads();
-  const int before = incl - h0 - h1 + (warp > 0 ? warp_sum[warp - 1] : 0);  // events larger than n0
-  // the start of a bucket in the descending order is the number of larger events
-  const int b0 = bucket_of(n0);
+  // events larger than size n_first - k, for each k
+  int before[kScanPerThread];
+  before[0] = incl - mine + (warp > 0 ? warp_sum[warp - 1] : 0);
+  for (int k = 1; k < kScanPerThread; ++k) before[k] = before[k - 1] + h[k - 1];
+  // the start of a bucket in the descending order is the number of larger
+  // events; sizes 256 << b are the largest of bucket b
   __shared__ int32_t bucket_start[kNumBuckets + 1];
-  // sizes 256 << b are the largest of bucket b: their "before" is the bucket start
-  for (int b = 0; b < kNumBuckets; ++b)
-    if (n0 == (256 << b)) bucket_start[b] = before;
-    else if (n1 == (256 << b)) bucket_start[b] = before + h0;
+  for (int k = 0; k < kScanPerThread; ++k)
+    for (int b = 0; b < kNumBuckets; ++b)
+      if (n_first - k == (256 << b)) bucket_start[b] = before[k];
   if (tid == 0) bucket_start[kNumBuckets] = 0;
   __syncthreads();
   const int total = warp_sum[31];
-  hist[n0] = before - bucket_start[b0];
-  if (n1 >= 1) hist[n1] = before + h0 - bucket_start[bucket_of(n1)];
+  for (int k = 0; k < kScanPerThread; ++k) {
+    const int n = n_first - k;
+    if (n >= 1) hist[n] = before[k] - bucket_start[bucket_of(n)];
+  }
   if (tid < kNumBuckets) {
     // bucket b spans positions [start_b, start_{b-1}) of the descending order
     const int hi = bucket_start[tid];
@@ -158,10 +154,10 @@ static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_e
   return cudaGetLastError();
 }
 
-// The large list: one CTA per event, at most two per SM (the events are
+// The large list: one CTA per event, a few per SM at most (the events are
 // few and long; the small buckets fill the rest of each SM).
 static cudaError_t launch_large(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
-                                cudaStream_t s) {
+                                const Tuning& tune, cudaStream_t s) {
   if (!sc.large_ws) return cudaSuccess;
   BatchArgs A = base;
   A.order = sc.order + kLargeQueue * sc.cap_events;
@@ -170,63 +166,58 @@ static cudaError_t launch_large(const BatchArgs& base, const Scratch& sc, int n_
   A.ws = sc.ws;
   A.ws_stride = sc.ws_stride;
   A.large_ws = sc.large_ws;
-  int grid = 2 * num_sms;
+  A.tile_factor = tune.tile_factor;
+  int grid = tune.large_ctas_per_sm * num_sms;
   if (grid > n_events) grid = n_events;
   if (grid < 1) grid = 1;
   k_cluster_tiled<<<grid, kTiledT, 0, s>>>(A);
   return cudaGetLastError();
 }
 
-template <int T, int SPT>
-static cudaError_t launch_bucket(const BatchArgs& A, int grid, cudaStream_t s) {
-  const size_t smem = sizeof(SmemLayout<T, SPT>);
-  // the attribute is per device: set it once for each device this process uses
-  static bool configured[64] = {};
+bool tuning_valid(const Tuning& t) {
+  for (int b = 0; b < kNumBuckets; ++b) {
+    const int v = t.bucket[b].variant;
+    if (v < 0 || v >= kNumVariants) return false;
+    const VariantShape sh = variant_shape(v);
+    if (sh.threads * sh.spt != (256 << b)) return false;
+    if (t.bucket[b].ctas_per_sm < 0 || t.bucket[b].ctas_per_sm > 64) return false;
+  }
+  return t.large_ctas_per_sm >= 1 && t.large_ctas_per_sm <= 8 && t.tile_factor >= 1.0 && t.tile_factor <= 8.0;
+}
+
+cudaError_t launch_variant(int v, const BatchArgs& A, int grid, cudaStream_t s) {
+  cudaError_t err = launch_variant_small(v, A, grid, s);
+  if (err == cudaErrorInvalidValue) err = launch_variant_large(v, A, grid, s);
+  return err;
+}
+
+int variant_occupancy(int v) {
+  static int cache[64][kNumVariants] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || !configured[dev]) {
-    cudaError_t err = cudaFuncSetAttribute(k_cluster_smem<T, SPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
-    if (err != cudaSuccess) return err;
-    if (dev >= 0 && dev < 64) configured[dev] = true;
-  }
-  k_cluster_smem<T, SPT><<<grid, T, smem, s>>>(A);
-  return cudaGetLastError();
+  int* slot = (dev >= 0 && dev < 64 && v >= 0 && v < kNumVariants) ? &cache[dev][v] : nullptr;
+  if (slot && *slot > 0) return *slot;
+  int nb = occupancy_variant_small(v);
+  if (nb < 0) nb = occupancy_variant_large(v);
+  if (nb < 1) nb = 1;
+  if (slot) *slot = nb;
+  return nb;
 }
 
-template <int T, int SPT>
-static int blocks_per_sm() {
-  int nb = 0;
-  const size_t smem = sizeof(SmemLayout<T, SPT>);
-  cudaFuncSetAttribute(k_cluster_smem<T, SPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cluster_smem<T, SPT>, T, smem) != cudaSuccess) nb = 1;
-  return nb < 1 ? 1 : nb;
+// Persistent grid of bucket b: the configured CTAs per SM, at most what fits,
+// at most one CTA per event.
+static int bucket_grid(const Tuning& tune, int b, int num_sms, int n_events) {
+  const int v = tune.bucket[b].variant;
+  const int fit = variant_occupancy(v);
+  int per_sm = tune.bucket[b].ctas_per_sm;
+  if (per_sm <= 0 || per_sm > fit) per_sm = fit;
+  int grid = num_sms * per_sm;
+  if (grid > n_events) grid = n_events;
+  return grid < 1 ? 1 : grid;
 }
 
-static cudaError_t launch_bucket_dispatch(int b, const BatchArgs& A, int grid, cudaStream_t s) {
-  switch (b) {
-    case 0: return launch_bucket<64, 4>(A, grid, s);
-    case 1: return launch_bucket<64, 8>(A, grid, s);
-    case 2: return launch_bucket<128, 8>(A, grid, s);
-    default: return launch_bucket<256, 8>(A, grid, s);
-  }
-}
-
-static int bucket_blocks_per_sm(int b) {
-  static int cache[kNumBuckets] = {0, 0, 0, 0};
-  if (cache[b] == 0) {
-    switch (b) {
-      case 0: cache[b] = blocks_per_sm<64, 4>(); break;
-      case 1: cache[b] = blocks_per_sm<64, 8>(); break;
-      case 2: cache[b] = blocks_per_sm<128, 8>(); break;
-      default: cache[b] = blocks_per_sm<256, 8>(); break;
-    }
-  }
-  return cache[b];
-}
-
-cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
-                         cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join) {
+cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, const Tuning& tune,
+                         cudaStream_t stream, cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join) {
   cudaError_t err = launch_sort(base, sc, n_events, stream);
   if (err != cudaSuccess) return err;
   if ((err = cudaEventRecord(*ev_fork, stream)) != cudaSuccess) return err;
@@ -234,7 +225,7 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
   {
     cudaStream_t s = side ? side[kLargeQueue] : stream;
     if (side && (err = cudaStreamWaitEvent(s, *ev_fork, 0)) != cudaSuccess) return err;
-    if ((err = launch_large(base, sc, n_events, num_sms, s)) != cudaSuccess) return err;
+    if ((err = launch_large(base, sc, n_events, num_sms, tune, s)) != cudaSuccess) return err;
     if (side) {
       if ((err = cudaEventRecord(ev_join[kLargeQueue], s)) != cudaSuccess) return err;
       if ((err = cudaStreamWaitEvent(stream, ev_join[kLargeQueue], 0)) != cudaSuccess) return err;
@@ -249,10 +240,9 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
     A.queue = sc.queues + b;
     A.ws = sc.ws;
     A.ws_stride = sc.ws_stride;
-    int grid = num_sms * bucket_blocks_per_sm(b);
-    if (grid > n_events) grid = n_events;
-    if (grid < 1) grid = 1;
-    if ((err = launch_bucket_dispatch(b, A, grid, s)) != cudaSuccess) return err;
+    if ((err = launch_variant(tune.bucket[b].variant, A, bucket_grid(tune, b, num_sms, n_events), s)) !=
+        cudaSuccess)
+      return err;
     if (side) {
       if ((err = cudaEventRecord(ev_join[b], s)) != cudaSuccess) return err;
       if ((err = cudaStreamWaitEvent(stream, ev_join[b], 0)) != cudaSuccess) return err;
@@ -262,10 +252,10 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
 }
 
 cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
-                                   cudaStream_t stream) {
+                                   const Tuning& tune, cudaStream_t stream) {
   cudaError_t err = launch_sort(base, sc, n_events, stream);
   if (err != cudaSuccess) return err;
-  if ((err = launch_large(base, sc, n_events, num_sms, stream)) != cudaSuccess) return err;
+  if ((err = launch_large(base, sc, n_events, num_sms, tune, stream)) != cudaSuccess) return err;
   for (int b = kNumBuckets - 1; b >= 0; --b) {
     BatchArgs A = base;
     A.order = sc.order + b * sc.cap_events;
@@ -273,10 +263,9 @@ cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int
     A.queue = sc.queues + b;
     A.ws = sc.ws;
     A.ws_stride = sc.ws_stride;
-    int grid = num_sms * bucket_blocks_per_sm(b);
-    if (grid > n_events) grid = n_events;
-    if (grid < 1) grid = 1;
-    if ((err = launch_bucket_dispatch(b, A, grid, stream)) != cudaSuccess) return err;
+    if ((err = launch_variant(tune.bucket[b].variant, A, bucket_grid(tune, b, num_sms, n_events), stream)) !=
+        cudaSuccess)
+      return err;
   }
   return cudaSuccess;
 }
@@ -291,7 +280,7 @@ __global__ void k_single_setup(int64_t* offsets1, int32_t* order, int32_t* count
   }
 }
 
-cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream) {
+cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, const Tuning& tune, cudaStream_t stream) {
   const int b = bucket_of(n);
   if (b < 0 && (!sc.large_ws || n > sc.large_ws_particles || n > kLargeMaxN)) return cudaErrorInvalidValue;
   k_single_setup<<<1, 1, 0, stream>>>(sc.offsets1, sc.order, sc.counts, sc.queues, n);
@@ -306,10 +295,11 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaS
   A.ws_stride = sc.ws_stride;
   if (b < 0) {
     A.large_ws = sc.large_ws;
+    A.tile_factor = tune.tile_factor;
     k_cluster_tiled<<<1, kTiledT, 0, stream>>>(A);
     return cudaGetLastError();
   }
-  return launch_bucket_dispatch(b, A, 1, stream);
+  return launch_variant(tune.bucket[b].variant, A, 1, stream);
 }
 
 __global__ void k_kinematics(const double* p4, int n, int algo, double* rap, double* phi, double* w) {

@@ -9,25 +9,67 @@
 namespace fjg {
 
 // Size buckets of the shared-memory path: bucket b holds events of up to
-// 256 << b particles, run by CTAs of 64, 64, 128, 256 threads (4, 8, 8, 8
-// slots per thread): 45 bytes of shared memory per slot and ~120 registers
-// per thread let 8, 8, 4 and 2 CTAs share an SM.
-constexpr int kNumBuckets = 4;
-constexpr int kSmemMaxN = 2048;
-// Events above kSmemMaxN particles form a fifth work list, run by the tiled
+// 256 << b particles (45 bytes of shared memory per slot; by default CTAs of
+// 64, 64, 128, 256 and 512 threads with 4, 8, 8, 8 and 8 slots per thread, of
+// which 8, 8, 4, 2 and 1 share an SM).
+constexpr int kNumBuckets = 5;
+constexpr int kSmemMaxN = 4096;
+// Events above kSmemMaxN particles form one more work list, run by the tiled
 // kernel (one CTA of 256 threads per event, state in the large workspace).
 constexpr int kLargeQueue = kNumBuckets;
 constexpr int kNumQueues = kNumBuckets + 1;
 constexpr int kLargeMaxN = 1 << 24;
 
 __host__ __device__ inline int bucket_of(int n) {
-  return n <= 256 ? 0 : n <= 512 ? 1 : n <= 1024 ? 2 : n <= 2048 ? 3 : -1;
+  return n <= 256 ? 0 : n <= 512 ? 1 : n <= 1024 ? 2 : n <= 2048 ? 3 : n <= 4096 ? 4 : -1;
 }
 
 // Status bits raised by kernels (ORed into the device status word).
 enum : int { kStatusTooBig = 1, kStatusBadArg = 2, kStatusInternal = 4 };
 
-static_assert(sizeof(SmemLayout<256, 8>) <= 232448 / 2, "bucket 3: two CTAs per SM");
+// Compiled variants of the shared-memory kernel: CTA size and slots per
+// thread (capacity = their product).  A bucket of capacity 256 << b can run
+// any variant of exactly that capacity.
+constexpr int kNumVariants = 11;
+struct VariantShape {
+  int threads, spt;
+};
+__host__ __device__ inline VariantShape variant_shape(int v) {
+  switch (v) {
+    case 0: return {64, 4};
+    case 1: return {128, 2};
+    case 2: return {64, 8};
+    case 3: return {128, 4};
+    case 4: return {256, 2};
+    case 5: return {128, 8};
+    case 6: return {256, 4};
+    case 7: return {256, 8};
+    case 8: return {512, 4};
+    case 9: return {512, 8};
+    case 10: return {256, 16};
+    default: return {0, 0};
+  }
+}
+
+// Launch configuration the autotuner chooses: per bucket a variant and the
+// CTAs per SM of its persistent grid (0: as many as fit), the CTAs per SM of
+// the tiled kernel, and its tile side in units of R (>= 1).
+struct BucketConfig {
+  int variant;
+  int ctas_per_sm;
+};
+struct Tuning {
+  BucketConfig bucket[kNumBuckets];
+  int large_ctas_per_sm;
+  double tile_factor;
+};
+inline Tuning default_tuning() { return Tuning{{{0, 0}, {2, 0}, {5, 0}, {7, 0}, {9, 0}}, 2, 1.0}; }
+bool tuning_valid(const Tuning& t);
+
+// Launch variant v (a persistent grid of `grid` CTAs); resident CTAs per SM of
+// variant v on the current device.
+cudaError_t launch_variant(int v, const BatchArgs& A, int grid, cudaStream_t s);
+int variant_occupancy(int v);
 
 // Device-side batch descriptor scratch owned by a context.
 struct Scratch {
@@ -49,17 +91,17 @@ constexpr int kHistBins = kSmemMaxN + 1;
 // Launch the bucketing kernels plus one persistent kernel per work list on
 // `stream` (the lists run concurrently on the kNumQueues side streams when
 // given).
-cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, cudaStream_t stream,
-                         cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join);
+cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms, const Tuning& tune,
+                         cudaStream_t stream, cudaStream_t* side, cudaEvent_t* ev_fork, cudaEvent_t* ev_join);
 
 // The bucketing kernels and the per-list kernels, all on `stream` one after
 // another (no side streams, no events).
 cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int n_events, int num_sms,
-                                   cudaStream_t stream);
+                                   const Tuning& tune, cudaStream_t stream);
 
 // One event, one CTA (the plain per-event-launch path; the tiled kernel above
 // kSmemMaxN particles).
-cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, cudaStream_t stream);
+cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, const Tuning& tune, cudaStream_t stream);
 
 // Scatter jets into the reference's PseudoJet records (in place).
 cudaError_t launch_pseudojet_epilogue(void* records, int size, const double* jets, const int32_t* jet_label,

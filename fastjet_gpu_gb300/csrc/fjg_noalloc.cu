@@ -124,7 +124,7 @@ extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t*
   // the array keeps the previous call's contents: clear the error word (the
   // launcher clears the bucket counters and queue heads)
   cudaError_t err = cudaMemsetAsync(sc.status, 0, sizeof(int32_t), s);
-  if (err == cudaSuccess) err = fjg::launch_batch_on_stream(A, sc, n_events, num_sms, s);
+  if (err == cudaSuccess) err = fjg::launch_batch_on_stream(A, sc, n_events, num_sms, fjg::default_tuning(), s);
   int st = 0;
   if (err == cudaSuccess) err = cudaMemcpyAsync(&st, sc.status, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);

@@ -134,6 +134,60 @@ fjg_status fjg_kinematics(fjg_ctx* ctx, const double* p4, int n, int algo, doubl
 fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int size, int algo, double r,
                                   void* stream);
 
+/* ------------------------------------------------------------ CUDA graphs
+ * No counterpart in the reference (one synchronous call per event).
+ *
+ * fjg_graph_capture_batch records one fjg_cluster_batch call on these device
+ * buffers (bucketing kernels, the per-bucket persistent kernels and the tiled
+ * kernel, with their fork/join across the context's side streams) as a CUDA
+ * graph.  n_events and total are fixed by the capture; the buffers' contents
+ * -- momenta, offsets (event sizes), per-event algorithms and radii -- may
+ * change between launches as long as offsets[n_events] <= total.  The graph
+ * owns its scratch, so graphs of one context may run concurrently on
+ * different streams; a graph's own launches must not overlap each other.  The
+ * context's tuning at capture time is baked in. */
+typedef struct fjg_graph fjg_graph;
+fjg_status fjg_graph_capture_batch(fjg_ctx* ctx, const double* p4, const int64_t* offsets, int n_events,
+                                   int64_t total, const int32_t* algo, int algo_all, const double* radius,
+                                   double r_all, const fjg_outputs* out, fjg_graph** graph);
+/* Launch on `stream` (NULL: the context's stream); asynchronous. */
+fjg_status fjg_graph_launch(fjg_graph* graph, void* stream);
+/* Wait for the last launch and report the kernels' status (FJG_ETOOBIG,
+ * FJG_EKERNEL, FJG_EINVAL for bad offsets); clears it. */
+fjg_status fjg_graph_check(fjg_graph* graph);
+void fjg_graph_destroy(fjg_graph* graph);
+
+/* ------------------------------------------------------------ autotuning
+ * No counterpart in the reference.  The batch launcher runs events of up to
+ * 256, 512, 1024, 2048 and 4096 particles (buckets 0-4) with one of several
+ * compiled kernel shapes each (CTA threads x slots per thread = the bucket's
+ * capacity) and a persistent grid of ctas_per_sm CTAs per SM (0: as many as
+ * fit); events above 4096 particles run on the tiled kernel with
+ * large_ctas_per_sm CTAs per SM and rapidity-azimuth tiles of side
+ * tile_factor * R (>= 1).  Every choice gives identical results; only the
+ * speed differs. */
+#define FJG_NUM_BUCKETS 5
+typedef struct {
+  int32_t threads[FJG_NUM_BUCKETS];          /* CTA size: 64 .. 512 */
+  int32_t slots_per_thread[FJG_NUM_BUCKETS]; /* threads * slots_per_thread = 256 << bucket */
+  int32_t ctas_per_sm[FJG_NUM_BUCKETS];      /* 0: the occupancy limit */
+  double events_per_s[FJG_NUM_BUCKETS];      /* the autotuner's measurement (0 when set by hand) */
+  int32_t large_ctas_per_sm;   /* 1 .. 8 */
+  double tile_factor;          /* 1 .. 8 */
+} fjg_tuning;
+
+fjg_status fjg_get_tuning(fjg_ctx* ctx, fjg_tuning* tuning);
+/* FJG_EINVAL if a (threads, slots_per_thread) pair is not one of the compiled
+ * shapes of that bucket's capacity or a field is out of range. */
+fjg_status fjg_set_tuning(fjg_ctx* ctx, const fjg_tuning* tuning);
+/* Time every compiled shape and a few CTA-per-SM counts on synthetic events
+ * of each bucket's size range (and, unless flags & FJG_TUNE_SKIP_LARGE, a few
+ * tile sides on events of 5000-9000 particles) for `algo` and `r`, keep the
+ * fastest, and return the choice in *result (may be NULL).  Takes about a
+ * second per bucket; synchronous. */
+#define FJG_TUNE_SKIP_LARGE 1
+fjg_status fjg_autotune(fjg_ctx* ctx, int algo, double r, int flags, fjg_tuning* result);
+
 /* Batched clustering that allocates no memory (no counterpart in the
  * reference, which allocates on every call).  For callers that cannot call
  * cudaMalloc at this point -- real-time or trigger code that forbids
@@ -153,7 +207,7 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
  * on the GPU race and must be serialised by the caller. */
 #define FJG_NOALLOC_MAX_EVENTS 65536
 #define FJG_NOALLOC_MAX_PARTICLES 131072
-#define FJG_NOALLOC_SCRATCH_BYTES ((7 * 8 + 96) * FJG_NOALLOC_MAX_PARTICLES + 5 * 4 * FJG_NOALLOC_MAX_EVENTS + 16384)
+#define FJG_NOALLOC_SCRATCH_BYTES ((7 * 8 + 96) * FJG_NOALLOC_MAX_PARTICLES + 6 * 4 * FJG_NOALLOC_MAX_EVENTS + 32768)
 fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t* offsets, int n_events, int64_t total,
                                      const int32_t* algo, int algo_all, const double* radius, double r_all,
                                      const fjg_outputs* out, void* stream);

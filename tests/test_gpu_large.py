@@ -1,4 +1,4 @@
-"""Events above 2048 particles (the tiled kernel) vs the CPU oracle (needs a GB300).
+"""Events above 4096 particles (the tiled kernel) vs the CPU oracle (needs a GB300).
 
 Sizes up to 20k particles are checked against the portable-kinematics oracle
 bit for bit (merge history with distances, jets, constituents).  The 10k-60k
@@ -42,7 +42,7 @@ def _check(ctx, ev, algo, radius, tag):
 
 @pytest.mark.parametrize("algo,radius", [(-1, 0.4), (1, 0.6), (0, 0.8), (-1, 0.1), (1, 1.5)])
 def test_large_events_bit_exact(ctx, algo, radius):
-    for n, seed in ((2049, 1), (3500, 2), (6000, 3)):
+    for n, seed in ((4097, 1), (5500, 2), (8000, 3)):
         _check(ctx, _pileup(n, seed), algo, radius, f"n={n} algo={algo} R={radius}")
 
 
@@ -55,15 +55,15 @@ def test_large_geometry_edges(ctx):
     """Narrow and wide rapidity ranges, rapidities beyond the tiled range,
     a single azimuth tile row, and the tile-count cap."""
     rng = np.random.default_rng(7)
-    n = 3000
+    n = 5000
     pt = rng.exponential(1.0, n) + 0.1
     phi = rng.uniform(-np.pi, np.pi, n)
     narrow = E._massless(pt, rng.uniform(-0.05, 0.05, n), phi)
     far = E._massless(pt, np.concatenate([rng.uniform(-4, 4, n - 40), rng.uniform(16, 30, 20),
                                           rng.uniform(-30, -16, 20)]), phi)
     strip = E._massless(pt, rng.uniform(-4, 4, n), rng.uniform(0.3, 0.35, n))
-    cases = [(narrow, -1, 0.4), (far, 1, 0.6), (strip, 0, 0.8), (_pileup(4000, 9), -1, 0.02),
-             (_pileup(2500, 10), -1, 3.5)]
+    cases = [(narrow, -1, 0.4), (far, 1, 0.6), (strip, 0, 0.8), (_pileup(6000, 9), -1, 0.02),
+             (_pileup(4500, 10), -1, 3.5)]
     for ci, (ev, algo, radius) in enumerate(cases):
         _check(ctx, ev, algo, radius, f"case {ci}")
 
@@ -71,7 +71,7 @@ def test_large_geometry_edges(ctx):
 def test_large_degenerate(ctx):
     """Repeated particles (one slot is the neighbour of hundreds of others:
     more targets than one pass lists), exact dR ties, zero-pT particles."""
-    base = _pileup(2600, 12)
+    base = _pileup(4300, 12)
     dup = np.concatenate([base, np.repeat(base[:3], 200, axis=0)])
     zero = base.copy()
     zero[::50, :2] = 0.0
@@ -81,10 +81,10 @@ def test_large_degenerate(ctx):
 
 
 def test_mixed_small_and_large_batch(ctx):
-    evs = [_pileup(n, 20 + k) for k, n in enumerate((120, 2048, 2049, 5000, 700, 3100, 1))]
+    evs = [_pileup(n, 20 + k) for k, n in enumerate((120, 2048, 4097, 5000, 700, 3100, 1, 4096))]
     b = E._batch_from(evs)
-    algo = np.array([-1, 1, 0, -1, 1, 0, -1], np.int32)
-    radius = np.array([0.4, 0.6, 0.8, 0.4, 1.0, 0.3, 0.4])
+    algo = np.array([-1, 1, 0, -1, 1, 0, -1, 1], np.int32)
+    radius = np.array([0.4, 0.6, 0.8, 0.4, 1.0, 0.3, 0.4, 0.5])
     res = ctx.cluster_batch(b.particles, b.offsets, algo, radius, history=True, owner=True)
     for e in range(b.n_events):
         o0, o1 = b.offsets[e], b.offsets[e + 1]
@@ -95,7 +95,7 @@ def test_mixed_small_and_large_batch(ctx):
 def test_plain_and_pseudojet_paths_large(ctx):
     import torch
     import fastjet_gpu_gb300 as F
-    ev = _pileup(4500, 30)
+    ev = _pileup(6000, 30)
     ref = _one(ctx, ev, -1, 0.4)
     one = ctx.cluster_event(torch.from_numpy(ev).cuda(), -1, 0.4, history=True)
     nj = int(one["n_jets"][0])

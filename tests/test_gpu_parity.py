@@ -58,7 +58,7 @@ def test_history_matches_oracle(ctx, algo, radius):
 
 
 def test_bucket_boundaries_and_tiny(ctx):
-    sizes = [0, 1, 2, 3, 31, 32, 33, 255, 256, 257, 511, 512, 513, 1023, 1024, 1025, 2047, 2048]
+    sizes = [0, 1, 2, 3, 31, 32, 33, 255, 256, 257, 511, 512, 513, 1023, 1024, 1025, 2047, 2048, 2049, 4095, 4096]
     evs = [E.single_event(n, 2, seed=n) if n else np.zeros((0, 4)) for n in sizes]
     p4, off = _batch(evs)
     for algo in (1, 0, -1):
