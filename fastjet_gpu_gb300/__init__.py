@@ -75,6 +75,19 @@ class _Tuning(ctypes.Structure):
 
 
 FJG_TUNE_SKIP_LARGE = 1
+FJG_SERVE_HISTORY = 1
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("arena_particles", ctypes.c_int64), ("max_inflight", ctypes.c_int32), ("streams", ctypes.c_int32),
+                ("max_batch", ctypes.c_int32), ("oversubscribe", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+class _Served(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_uint64), ("status", ctypes.c_int32), ("n_particles", ctypes.c_int32),
+                ("n_jets", ctypes.c_int32), ("jets", ctypes.POINTER(ctypes.c_double)),
+                ("jet_label", ctypes.POINTER(ctypes.c_int32)), ("history", ctypes.c_void_p),
+                ("owner", ctypes.POINTER(ctypes.c_int32)), ("latency_us", ctypes.c_double)]
 
 _lib = None
 
@@ -111,6 +124,14 @@ def lib():
         L.fjg_get_tuning.argtypes = [P, ctypes.POINTER(_Tuning)]
         L.fjg_set_tuning.argtypes = [P, ctypes.POINTER(_Tuning)]
         L.fjg_autotune.argtypes = [P, I, D, I, ctypes.POINTER(_Tuning)]
+        L.fjg_server_create.argtypes = [P, ctypes.POINTER(_ServerConfig), ctypes.POINTER(P)]
+        L.fjg_server_destroy.argtypes = [P]
+        L.fjg_server_destroy.restype = None
+        L.fjg_server_submit.argtypes = [P, P, I, I, D, ctypes.POINTER(ctypes.c_uint64)]
+        L.fjg_server_poll.argtypes = [P, ctypes.POINTER(_Served), I, ctypes.POINTER(I), ctypes.c_int64]
+        L.fjg_server_release.argtypes = [P, ctypes.c_uint64]
+        L.fjg_server_pending.argtypes = [P]
+        L.fjg_server_replay.argtypes = [P, P, P, I, P, P, P, P, ctypes.POINTER(D)]
         _lib = L
     return _lib
 
@@ -336,6 +357,77 @@ class Graph:
     def close(self):
         if self._h:
             lib().fjg_graph_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request server on a context (fjg_server_*): submit events one at a time,
+    poll for completed ones.  Continuous batching; see fastjet_gb300.h."""
+
+    def __init__(self, ctx, arena_particles=0, max_inflight=0, streams=0, max_batch=0, oversubscribe=0,
+                 history=False):
+        self.ctx = ctx
+        cfg = _ServerConfig(int(arena_particles), int(max_inflight), int(streams), int(max_batch),
+                            int(oversubscribe), FJG_SERVE_HISTORY if history else 0)
+        self._h = ctypes.c_void_p()
+        ctx._check(lib().fjg_server_create(ctx._h, ctypes.byref(cfg), ctypes.byref(self._h)))
+        self.history = history
+
+    def submit(self, p4, algo, radius):
+        p4 = np.ascontiguousarray(p4, dtype=np.float64).reshape(-1, 4)
+        t = ctypes.c_uint64()
+        self.ctx._check(lib().fjg_server_submit(self._h, _np_ptr(p4), p4.shape[0], int(algo), float(radius),
+                                                ctypes.byref(t)))
+        return t.value
+
+    def poll(self, max_results=64, timeout_us=0):
+        """Completed requests as dicts (results copied, arena ranges released)."""
+        buf = (_Served * max_results)()
+        n = ctypes.c_int()
+        self.ctx._check(lib().fjg_server_poll(self._h, buf, max_results, ctypes.byref(n), int(timeout_us)))
+        out = []
+        for k in range(n.value):
+            r = buf[k]
+            nj, npart = r.n_jets, r.n_particles
+            d = {"ticket": r.ticket, "status": r.status, "n_jets": nj, "latency_us": r.latency_us,
+                 "jets": np.ctypeslib.as_array(r.jets, (max(nj, 1) * 4,))[: 4 * nj].reshape(nj, 4).copy()
+                 if nj else np.zeros((0, 4)),
+                 "jet_label": np.ctypeslib.as_array(r.jet_label, (max(nj, 1),))[:nj].copy() if nj else
+                 np.zeros(0, np.int32)}
+            if self.history and npart:
+                raw = (ctypes.c_char * (16 * npart)).from_address(r.history)
+                d["history"] = np.frombuffer(raw, dtype=STEP, count=npart).copy()
+                d["owner"] = np.ctypeslib.as_array(r.owner, (npart,)).copy()
+            out.append(d)
+            self.ctx._check(lib().fjg_server_release(self._h, r.ticket))
+        return out
+
+    @property
+    def pending(self):
+        return lib().fjg_server_pending(self._h)
+
+    def replay(self, particles, offsets, algo, radius, arrival_us):
+        """Open-loop replay of a trace; returns (latency_us per event, wall_us)."""
+        p4 = np.ascontiguousarray(particles, dtype=np.float64)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        a = np.ascontiguousarray(algo, dtype=np.int32)
+        r = np.ascontiguousarray(radius, dtype=np.float64)
+        t = np.ascontiguousarray(arrival_us, dtype=np.float64)
+        lat = np.zeros(off.size - 1)
+        wall = ctypes.c_double()
+        self.ctx._check(lib().fjg_server_replay(self._h, _np_ptr(p4), _np_ptr(off), off.size - 1, _np_ptr(a),
+                                                _np_ptr(r), _np_ptr(t), _np_ptr(lat), ctypes.byref(wall)))
+        return lat, wall.value
+
+    def close(self):
+        if self._h:
+            lib().fjg_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -52,7 +52,7 @@ enum WsField { kRap = 0, kPhi, kW, kPx, kPy, kPz, kE, kWsFields };
 struct BatchArgs {
   const double* p4;        // particle s of event e: p4 + (offsets[e] + s) * p4_stride
   int p4_stride;           // doubles between consecutive particles (4 for [n][4], 5 for PseudoJet AoS)
-  const int64_t* offsets;  // [n_events + 1]
+  const int64_t* offsets;  // [n_events + 1] (CSR), or [2 n_events] (start, end) pairs when pairs != 0
   const int32_t* algo;     // [n_events] or null
   const double* radius;    // [n_events] or null
   int algo_all;
@@ -70,7 +70,30 @@ struct BatchArgs {
   int* status;             // device error flag (0 = ok)
   unsigned char* large_ws; // tiled-path workspace: event e at large_ws + 96 * offsets[e] (null: none)
   double tile_factor;      // tiled path: tile side >= tile_factor * R (>= 1)
+  int pairs;               // offsets hold (start, end) pairs: events need not be contiguous
+  int* done;               // null, or completion flags: done[done_slot[e]] = 1 (system scope) per event
+  const int32_t* done_slot;
 };
+
+// Particle range [off, off + N) of event e.
+__device__ __forceinline__ void event_range(const BatchArgs& A, int e, int64_t& off, int& N) {
+  if (A.pairs) {
+    off = A.offsets[2 * (int64_t)e];
+    N = (int)(A.offsets[2 * (int64_t)e + 1] - off);
+  } else {
+    off = A.offsets[e];
+    N = (int)(A.offsets[e + 1] - off);
+  }
+}
+
+// After the last write of event e (call after a block barrier, one thread):
+// make the event's outputs visible system-wide, then raise its flag.
+__device__ __forceinline__ void signal_done(const BatchArgs& A, int e) {
+  if (!A.done) return;
+  __threadfence_system();
+  int* flag = A.done + A.done_slot[e];
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
+}
 
 constexpr int kRescanChunk = 8;  // targets per register pass
 constexpr int kMaxTargets = 32;  // targets per step scanned during the merge
@@ -306,9 +329,9 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
   constexpr int MW = (T >= 128) ? 3 : 1;  // merge warps
   constexpr int TR = T - 32 * MW;         // rescan threads
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t off = A.offsets[e];
+  int64_t off;
   EventCtx X;
-  X.N = (int)(A.offsets[e + 1] - off);
+  event_range(A, e, off, X.N);
   X.algo = A.algo ? A.algo[e] : A.algo_all;
   const double R = A.radius ? A.radius[e] : A.r_all;
   X.inv_r2 = 1.0 / (R * R);

@@ -415,9 +415,9 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   constexpr int MW = 3;
   constexpr int TR = T - 32 * MW;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t off = A.offsets[e];
+  int64_t off;
   EventCtx X;
-  X.N = (int)(A.offsets[e + 1] - off);
+  event_range(A, e, off, X.N);
   X.algo = A.algo ? A.algo[e] : A.algo_all;
   const double R = A.radius ? A.radius[e] : A.r_all;
   X.inv_r2 = 1.0 / (R * R);

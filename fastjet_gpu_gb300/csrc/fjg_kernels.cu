@@ -17,7 +17,13 @@ __global__ void __launch_bounds__(kTiledT) k_cluster_tiled(BatchArgs A) {
     const int e = S.event;
     if (e < 0) break;
     cluster_event_tiled(S, A, A.large_ws, e);  // ends with a barrier
+    if (threadIdx.x == 0) signal_done(A, e);
   }
+}
+
+cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
+  k_cluster_tiled<<<grid < 1 ? 1 : grid, kTiledT, 0, s>>>(A);
+  return cudaGetLastError();
 }
 
 // Events are handed to the bucket kernels largest first (longest-processing-

@@ -66,6 +66,9 @@ struct Tuning {
 inline Tuning default_tuning() { return Tuning{{{0, 0}, {2, 0}, {5, 0}, {7, 0}, {9, 0}}, 2, 1.0}; }
 bool tuning_valid(const Tuning& t);
 
+// The tiled kernel over the work list of A (a persistent grid of `grid` CTAs).
+cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s);
+
 // Launch variant v (a persistent grid of `grid` CTAs); resident CTAs per SM of
 // variant v on the current device.
 cudaError_t launch_variant(int v, const BatchArgs& A, int grid, cudaStream_t s);

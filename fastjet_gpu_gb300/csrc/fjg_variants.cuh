@@ -22,6 +22,7 @@ __global__ void __launch_bounds__(T) k_cluster_smem(BatchArgs A) {
     const int e = S.event;
     if (e < 0) break;
     cluster_event_smem<T, SPT>(S, A, e);  // ends with a barrier
+    if (threadIdx.x == 0) signal_done(A, e);
   }
 }
 

@@ -188,6 +188,73 @@ fjg_status fjg_set_tuning(fjg_ctx* ctx, const fjg_tuning* tuning);
 #define FJG_TUNE_SKIP_LARGE 1
 fjg_status fjg_autotune(fjg_ctx* ctx, int algo, double r, int flags, fjg_tuning* result);
 
+/* ------------------------------------------------------------ serving
+ * No counterpart in the reference.  A request server on one context: events
+ * are submitted one at a time as they arrive and complete independently.
+ *
+ * - State: a particle arena of `arena_particles` entries.  An admitted event
+ *   holds a contiguous range of it: its momenta and results in pinned host
+ *   memory that the kernels read and write directly, its clustering state
+ *   (the FP64 workspace, and the tiled kernel's workspace above 4096
+ *   particles) in device memory.  Admission is first come, first served, by
+ *   arena space (the HBM footprint) and by the resident CTA slots of the
+ *   event's size bucket (the shared-memory footprint, oversubscribed by at
+ *   most `oversubscribe`).
+ * - Continuous batching: admitted events of one size bucket are launched
+ *   together as a micro-batch on the first idle stream of a pool of
+ *   `streams`, while earlier micro-batches are still running; every event
+ *   raises its own completion flag in mapped host memory as soon as it is
+ *   done, so results do not wait for the rest of their micro-batch.
+ * - Progress happens inside fjg_server_submit and fjg_server_poll (no
+ *   background thread); a server is driven by one host thread at a time.
+ * Results are identical to fjg_cluster_batch on the same event. */
+typedef struct fjg_server fjg_server;
+typedef struct {
+  int64_t arena_particles; /* default 4194304 */
+  int32_t max_inflight;    /* events admitted and not yet released; default 8192 */
+  int32_t streams;         /* micro-batch streams; default 16 */
+  int32_t max_batch;       /* events per micro-batch; default 512 */
+  int32_t oversubscribe;   /* launched events per resident CTA slot of a bucket; default 2 */
+  int32_t flags;           /* FJG_SERVE_HISTORY: also return the merge history and constituents */
+} fjg_server_config;
+#define FJG_SERVE_HISTORY 1
+
+/* One completed request.  The pointers are into the server's arena and stay
+ * valid until fjg_server_release(ticket). */
+typedef struct {
+  uint64_t ticket;
+  int32_t status;          /* FJG_OK or the kernel's error */
+  int32_t n_particles;
+  int32_t n_jets;
+  const double* jets;      /* [n_jets][4], in promotion order */
+  const int32_t* jet_label;
+  const fjg_step* history; /* [n_particles] or NULL */
+  const int32_t* owner;    /* [n_particles] or NULL */
+  double latency_us;       /* from submission to the completion being observed */
+} fjg_served;
+
+/* config may be NULL (defaults); zero fields take their defaults. */
+fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_server** server);
+void fjg_server_destroy(fjg_server* server);
+/* Queue one event (host memory, [n][4] px py pz E; copied); FJG_EINVAL for
+ * bad arguments, FJG_ETOOBIG when it can never fit the arena. */
+fjg_status fjg_server_submit(fjg_server* server, const double* p4, int n, int algo, double r, uint64_t* ticket);
+/* Make progress and return up to `max` completed requests; waits up to
+ * timeout_us microseconds for the first one (0: do not wait). */
+fjg_status fjg_server_poll(fjg_server* server, fjg_served* out, int max, int* n_out, int64_t timeout_us);
+/* Free the arena range of a returned request. */
+fjg_status fjg_server_release(fjg_server* server, uint64_t ticket);
+/* Submitted and not yet returned by fjg_server_poll. */
+int fjg_server_pending(const fjg_server* server);
+/* Open-loop replay of a request trace (benchmarking): event i (CSR p4 and
+ * offsets in host memory, algo[i], radius[i]) is submitted at arrival_us[i]
+ * microseconds after the start, results are released as they complete, and
+ * latency_us[i] receives the time from the scheduled arrival to the observed
+ * completion.  *wall_us receives the time to the last completion. */
+fjg_status fjg_server_replay(fjg_server* server, const double* p4, const int64_t* offsets, int n_events,
+                             const int32_t* algo, const double* radius, const double* arrival_us,
+                             double* latency_us, double* wall_us);
+
 /* Batched clustering that allocates no memory (no counterpart in the
  * reference, which allocates on every call).  For callers that cannot call
  * cudaMalloc at this point -- real-time or trigger code that forbids
