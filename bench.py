@@ -51,6 +51,14 @@ WORKLOADS = {
         workload="64 pile-up-like events, 10k-60k particles, anti-kt R=0.4 (kt R=0.6 beside it), FP64, "
                  "one batched call"),
 }
+WORKLOADS["serving"] = dict(
+    events=3000, make=lambda n: E.serving_mix(n, seed=5)[0], flush=False, cpu_start=32, per_event_sample=64,
+    second=None,
+    metric="events/s served, open-loop Poisson arrivals of single events (lognormal sizes, median 1500), "
+           "with p50/p99 latency",
+    workload="served requests: sizes lognormal (median 1500, sigma 0.8) clipped to [100, 20000]; anti-kt R=0.4 "
+             "70%, kt R=0.6 15%, C/A R=0.8 15%; Poisson arrivals at 20k-200k events/s")
+SERVING_RATES = (20000, 50000, 100000, 200000)
 W = WORKLOADS["mixed"]
 N_EVENTS = W["events"]
 METRIC = W["metric"]
@@ -330,6 +338,91 @@ def run_ours(args, rank, world, local_rank):
     ctx.close()
 
 
+def run_serving(args, rank, world, local_rank):
+    """Open-loop serving: each offered rate replays the same request trace
+    (one event per request) through the server; latency runs from each
+    request's scheduled arrival to its completion being observed."""
+    import torch
+
+    import fastjet_gpu_gb300 as F
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local_rank)
+    batch, algo, radius = E.serving_mix(N_EVENTS, seed=5)
+    sizes = batch.sizes()
+    small = sizes <= 2000
+    ctx = F.Context(local_rank)
+    tuning = None if args.no_tune else ctx.autotune(-1, 0.4)
+    srv = F.Server(ctx)
+    rng = np.random.default_rng(17)
+    gaps = rng.exponential(1.0, N_EVENTS)
+    # warm-up: the first requests of the trace, well spaced
+    for _ in range(max(args.warmup, 3)):
+        k = min(256, N_EVENTS)
+        srv.replay(batch.particles[: batch.offsets[k]], batch.offsets[: k + 1], algo[:k], radius[:k],
+                   np.arange(k) * 50.0)
+    rates = []
+    with ClockSampler(local_rank) as clk:
+        for rate in SERVING_RATES:
+            arrival = np.cumsum(gaps) * (1e6 / rate)
+            lat, wall = srv.replay(batch.particles, batch.offsets, algo, radius, arrival)
+            rates.append({"offered": rate, "served": N_EVENTS / (wall * 1e-6), "wall_s": wall * 1e-6,
+                          "p50_ms": float(np.percentile(lat, 50)) / 1e3, "p99_ms": float(np.percentile(lat, 99)) / 1e3,
+                          "p50_ms_le2000": float(np.percentile(lat[small], 50)) / 1e3,
+                          "p99_ms_le2000": float(np.percentile(lat[small], 99)) / 1e3})
+    # lightly loaded: requests one at a time (latency of a lone event)
+    lone_idx = np.linspace(0, N_EVENTS - 1, 64).astype(int)
+    lone = []
+    for e in lone_idx:
+        t0 = time.perf_counter()
+        srv.submit(batch.event(int(e)), int(algo[e]), float(radius[e]))
+        got = []
+        while not got:
+            got = srv.poll(1, timeout_us=1000000)
+        lone.append(1e3 * (time.perf_counter() - t0))
+    lone = np.array(lone)
+    lone_small = lone[sizes[lone_idx] <= 2000]
+    srv.close()
+    # the same events as one batch, and one event per launch
+    dev = torch.device("cuda", local_rank)
+    p4 = torch.from_numpy(batch.particles).to(dev)
+    off = torch.from_numpy(batch.offsets).to(dev)
+    a_t = torch.from_numpy(algo).to(dev)
+    r_t = torch.from_numpy(radius).to(dev)
+    ctx.cluster_batch_device(p4, off, a_t, r_t)
+    ctx.check()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.cluster_batch_device(p4, off, a_t, r_t)
+    ctx.check()
+    batched = N_EVENTS / (time.perf_counter() - t0)
+    sample = [torch.from_numpy(batch.event(int(e))).to(dev) for e in lone_idx[:16]]
+    t0 = time.perf_counter()
+    for k, ev in enumerate(sample):
+        e = int(lone_idx[k])
+        ctx.cluster_event(ev, int(algo[e]), float(radius[e]))
+    per_event = len(sample) / (time.perf_counter() - t0)
+    top = rates[-1]
+    h2d = int(batch.particles.nbytes)
+    line = {"metric": METRIC, "value": top["served"], "unit": "events/s", "n_gpus": 1, "steps": len(SERVING_RATES),
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * float(np.mean([r["wall_s"] for r in rates])),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "requests_per_rate": N_EVENTS, "particles": int(batch.offsets[-1]),
+                       "rates": rates, "tuning": tuning,
+                       "lone_request_ms": {"p50": float(np.percentile(lone, 50)), "p99": float(np.percentile(lone, 99)),
+                                           "p50_le2000": float(np.percentile(lone_small, 50)),
+                                           "p99_le2000": float(np.percentile(lone_small, 99)),
+                                           "sample": f"{len(lone)} requests one at a time"},
+                       "batched_same_events": batched, "per_event_launch": per_event},
+            "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+            "e2e": {"value": top["served"], "unit": "events/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 0},
+            "gpu_launches": None, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -350,6 +443,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "serving":
+        run_serving(args, rank, world, local_rank)
         return
     if world > 1:
         import torch
