@@ -430,7 +430,11 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
     // S1: argmin over (klo, label) with a certificate.  The winner's neighbour
     // and kind travel with the reduction: once B1 is passed the merge warps
     // may overwrite the winner's slot (compaction) while other warps are still
-    // deciding what to do.
+    // deciding what to do.  The certificate's second-smallest bound m2 leaves
+    // out the best candidate's mutual partner: two slots that are each other's
+    // neighbour with pair keys hold the same exact key (the same FP64
+    // expression of the same pair), and whichever of them is taken, the step
+    // merges that pair, so their tie needs no FP64 resolution.
     Cert mine = cert_empty();
     int mlab = 0x7fffffff, mnn = -1, mpair = 0;
     for (int k = 0; k < SPT; ++k) {
@@ -439,15 +443,18 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       const float lo = S.klo[t];
       const int l = S.label[t];
       if (lo < mine.m1 || (lo == mine.m1 && l < mlab)) {
-        mine.m2 = mine.m1;
+        const int tnn = S.nn[t], tpair = S.pair[t];
+        const bool partners = tpair && mpair && tnn == mine.i1 && mnn == t;
+        mine.m2 = partners ? mine.m2 : mine.m1;
         mine.m1 = lo;
         mine.u1 = S.khi[t];
         mine.i1 = t;
         mlab = l;
-        mnn = S.nn[t];
-        mpair = S.pair[t];
+        mnn = tnn;
+        mpair = tpair;
       } else {
-        mine.m2 = fminf(mine.m2, lo);
+        const bool partners = mpair && t == mnn && S.pair[t] && S.nn[t] == mine.i1;
+        if (!partners) mine.m2 = fminf(mine.m2, lo);
       }
     }
     {
@@ -462,10 +469,12 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       wc.i1 = __shfl_sync(kFull, mine.i1, src);
       wc.u1 = __shfl_sync(kFull, mine.u1, src);
       if (!ball) wc.i1 = -1;
-      const unsigned other = (ball && lane == src) ? __float_as_uint(mine.m2) : __float_as_uint(mine.m1);
-      wc.m2 = __uint_as_float(__reduce_min_sync(kFull, other));
       const int wnn = __shfl_sync(kFull, mnn, src);
       const int wpair = __shfl_sync(kFull, mpair, src);
+      const bool partners = ball && mpair && wpair && mnn == wc.i1 && wnn == mine.i1;
+      const unsigned other = (ball && lane == src) ? __float_as_uint(mine.m2)
+                                                   : __float_as_uint(partners ? mine.m2 : mine.m1);
+      wc.m2 = __uint_as_float(__reduce_min_sync(kFull, other));
       if (lane == 0) {
         S.warg[warp] = wc;
         S.wlab[warp] = ball ? (int)lb : 0x7fffffff;
@@ -492,7 +501,9 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       u1 = __shfl_sync(kFull, x.u1, src);
       cnn = __shfl_sync(kFull, xnn, src);
       cpair = __shfl_sync(kFull, xpair, src);
-      const unsigned other = (ball && lane == src) ? __float_as_uint(x.m2) : __float_as_uint(x.m1);
+      const bool partners = ball && xpair && cpair && xnn == c && cnn == x.i1;
+      const unsigned other = (ball && lane == src) ? __float_as_uint(x.m2)
+                                                   : __float_as_uint(partners ? x.m2 : x.m1);
       const float m2 = __uint_as_float(__reduce_min_sync(kFull, other));
       certified = (c >= 0) && (u1 < m2);
     }
