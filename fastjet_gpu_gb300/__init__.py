@@ -124,6 +124,8 @@ def lib():
         L.fjg_get_tuning.argtypes = [P, ctypes.POINTER(_Tuning)]
         L.fjg_set_tuning.argtypes = [P, ctypes.POINTER(_Tuning)]
         L.fjg_autotune.argtypes = [P, I, D, I, ctypes.POINTER(_Tuning)]
+        L.fjg_select_jets.argtypes = [P, P, P, P, P, I, ctypes.c_int64, D, I, P, P, P, P]
+        L.fjg_combine_events.argtypes = [P, P, I, I, P, ctypes.POINTER(I), P]
         L.fjg_server_create.argtypes = [P, ctypes.POINTER(_ServerConfig), ctypes.POINTER(P)]
         L.fjg_server_destroy.argtypes = [P]
         L.fjg_server_destroy.restype = None
@@ -144,8 +146,30 @@ def _t_ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+_CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
+
+
+def _torch_stream(stream, device):
+    """The stream a device-tensor call runs on: the given handle, or torch's
+    current stream, so that torch's copies, reads and frees of the tensors
+    are ordered with the library's kernels."""
+    if stream:
+        return stream
+    import torch
+    h = torch.cuda.current_stream(device).cuda_stream
+    # torch's default stream has handle 0, which the C API reads as "the
+    # context's stream": pass the explicit legacy-default-stream handle instead
+    return h if h else _CUDA_STREAM_LEGACY
+
+
 class Context:
-    """A library context on one CUDA device (stream, scratch, side streams)."""
+    """A library context on one CUDA device (stream, scratch, side streams).
+
+    Calls on torch CUDA tensors run on torch's current stream unless a stream
+    handle is given; the synchronous ones (``cluster_event``,
+    ``cluster_pseudojets``, ``kinematics``) run on the context's stream after
+    it has waited for torch's current stream.
+    """
 
     def __init__(self, device=0):
         self._h = ctypes.c_void_p()
@@ -176,6 +200,11 @@ class Context:
 
     def check(self):
         self._check(lib().fjg_ctx_check(self._h))
+
+    def _after_torch(self, device):
+        """Make the context's stream wait for torch's current stream."""
+        import torch
+        torch.cuda.ExternalStream(self.stream, device=device).wait_stream(torch.cuda.current_stream(device))
 
     # ------------------------------------------------------------ host memory
     def cluster_batch(self, particles, offsets, algo, radius, history=False, owner=False):
@@ -239,10 +268,10 @@ class Context:
                      out["owner"].data_ptr() if "owner" in out else None)
         a_t = None if isinstance(algo, (int, np.integer)) else algo
         r_t = None if isinstance(radius, (float, int, np.floating)) else radius
+        s = _torch_stream(stream, p4.device)
         st = lib().fjg_cluster_batch(self._h, _t_ptr(p4), _t_ptr(offsets), ne, int(total), _t_ptr(a_t),
                                      int(algo) if a_t is None else 0, _t_ptr(r_t),
-                                     float(radius) if r_t is None else 0.0, ctypes.byref(o),
-                                     ctypes.c_void_p(stream) if stream else None)
+                                     float(radius) if r_t is None else 0.0, ctypes.byref(o), ctypes.c_void_p(s))
         self._check(st)
         return out
 
@@ -294,6 +323,35 @@ class Context:
                                        ctypes.byref(t)))
         return t.to_dict()
 
+    def select_jets(self, out, offsets, ptmin=0.0, sort=True, total=None, stream=None):
+        """Inclusive jets with pT >= ptmin per event, by decreasing pT (device).
+
+        ``out`` holds a batch's device outputs (``jets``, ``jet_label``,
+        ``n_jets``); returns new tensors at the same positions.
+        """
+        import torch
+        ne = offsets.numel() - 1
+        total = out["jets"].shape[0] if total is None else total
+        dev = out["jets"].device
+        res = {"jets": torch.empty_like(out["jets"]), "jet_label": torch.empty_like(out["jet_label"]),
+               "n_jets": torch.empty(max(ne, 1), dtype=torch.int32, device=dev)}
+        self._check(lib().fjg_select_jets(self._h, _t_ptr(out["jets"]), _t_ptr(out["jet_label"]),
+                                          _t_ptr(out["n_jets"]), _t_ptr(offsets), ne, int(total), float(ptmin),
+                                          1 if sort else 0, _t_ptr(res["jets"]), _t_ptr(res["jet_label"]),
+                                          _t_ptr(res["n_jets"]), ctypes.c_void_p(_torch_stream(stream, dev))))
+        return res
+
+    def combine_events(self, offsets, k, stream=None):
+        """Offsets of the batch with every k consecutive events merged (k = 0: all)."""
+        import torch
+        ne = offsets.numel() - 1
+        n_out = ctypes.c_int()
+        res = torch.empty(max(ne, 1) + 1, dtype=torch.int64, device=offsets.device)
+        self._check(lib().fjg_combine_events(self._h, _t_ptr(offsets), ne, int(k), _t_ptr(res),
+                                             ctypes.byref(n_out),
+                                             ctypes.c_void_p(_torch_stream(stream, offsets.device))))
+        return res[: n_out.value + 1]
+
     def cluster_event(self, p4, algo, radius, history=False, owner=False):
         """The plain path: one event per launch (torch CUDA tensors), synchronous."""
         import torch
@@ -306,6 +364,7 @@ class Context:
             out["history"] = torch.empty((max(n, 1), 2), dtype=torch.float64, device=dev)
         if owner:
             out["owner"] = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        self._after_torch(dev)
         st = lib().fjg_cluster_event(self._h, _t_ptr(p4), n, int(algo), float(radius), _t_ptr(out["jets"]),
                                      _t_ptr(out["jet_label"]), _t_ptr(out["n_jets"]),
                                      _t_ptr(out.get("history")), _t_ptr(out.get("owner")))
@@ -317,6 +376,7 @@ class Context:
         import torch
         n = p4.shape[0]
         rap, phi, w = (torch.empty(max(n, 1), dtype=torch.float64, device=p4.device) for _ in range(3))
+        self._after_torch(p4.device)
         self._check(lib().fjg_kinematics(self._h, _t_ptr(p4), n, int(algo), _t_ptr(rap), _t_ptr(phi), _t_ptr(w),
                                          None))
         self.check()
@@ -335,6 +395,7 @@ class Context:
             dev = torch.from_numpy(records.view(np.uint8).reshape(-1).copy()).cuda(self.device)
         else:
             host, dev = None, records
+        self._after_torch(dev.device)
         st = lib().fjg_cluster_pseudojets(self._h, _t_ptr(dev), int(size), int(algo), float(radius), None)
         self._check(st)
         if host is not None:
@@ -349,7 +410,9 @@ class Graph:
         self.ctx, self._h, self.out, self._keep = ctx, handle, out, keep
 
     def launch(self, stream=None):
-        self.ctx._check(lib().fjg_graph_launch(self._h, ctypes.c_void_p(stream) if stream else None))
+        """Launch on the given stream handle, or torch's current stream."""
+        s = _torch_stream(stream, self.out["jets"].device)
+        self.ctx._check(lib().fjg_graph_launch(self._h, ctypes.c_void_p(s)))
 
     def check(self):
         self.ctx._check(lib().fjg_graph_check(self._h))

@@ -171,6 +171,7 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
   ctx->scratch.release();
   ctx->io.release();
   ctx->single.release();
+  ctx->select_scratch.release();
   delete ctx;
 }
 

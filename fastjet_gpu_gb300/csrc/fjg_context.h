@@ -80,6 +80,7 @@ struct fjg_ctx {
   fjg::ScratchSet scratch;  // the context's own launches
   fjg::DeviceBuffer io;     // device copies for the host-memory entry points
   fjg::DeviceBuffer single; // outputs of fjg_cluster_pseudojets
+  fjg::DeviceBuffer select_scratch;  // fjg_select_jets: sort keys of events with many jets
   fjg::Tuning tune = fjg::default_tuning();
   double tuned_rate[fjg::kNumBuckets] = {};
   std::string last_error;

@@ -134,6 +134,26 @@ fjg_status fjg_kinematics(fjg_ctx* ctx, const double* p4, int n, int algo, doubl
 fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int size, int algo, double r,
                                   void* stream);
 
+/* ------------------------------------------------------------ epilogue
+ * Replaces the reference driver's host post-processing (main.cc:309-327):
+ * per event, keep the inclusive jets with px*px + py*py >= ptmin^2 and, when
+ * `sort` is nonzero, order them by decreasing pt^2 (equal pt^2 by increasing
+ * jet label; the reference's std::sort leaves that order unspecified).
+ * Inputs are a batch's outputs (device memory, CSR by `offsets`, `total` =
+ * offsets[n_events]); outputs go to the same positions of out_jets /
+ * out_label, with the kept count in out_n_jets.  Stream-ordered. */
+fjg_status fjg_select_jets(fjg_ctx* ctx, const double* jets, const int32_t* jet_label, const int32_t* n_jets,
+                           const int64_t* offsets, int n_events, int64_t total, double ptmin, int sort,
+                           double* out_jets, int32_t* out_label, int32_t* out_n_jets, void* stream);
+
+/* The driver's --combine k (main.cc:76-85, 269) on a device CSR batch: every
+ * k consecutive events become one (k = 0: all of them), which only changes
+ * the offsets -- out_offsets[i] = offsets[min(i k, n_events)] for
+ * i = 0 .. *n_out, with *n_out = ceil(n_events / k).  Stream-ordered;
+ * *n_out is known on return. */
+fjg_status fjg_combine_events(fjg_ctx* ctx, const int64_t* offsets, int n_events, int k, int64_t* out_offsets,
+                              int* n_out, void* stream);
+
 /* ------------------------------------------------------------ CUDA graphs
  * No counterpart in the reference (one synchronous call per event).
  *
