@@ -296,9 +296,13 @@ __device__ __forceinline__ void rescan_chunk(SmemLayout<T, SPT>& S, const EventC
   }
 }
 
-// Named barriers: 1 among the rescan warps, 2 among the merge warps.
+// Named barriers: 1 among the rescan warps, 2 among the merge warps.  The
+// non-aligned form: the compiler does not see an inline-asm barrier as a
+// point where a warp must reconverge, and the threads of a warp may reach it
+// apart (after loops whose trip counts differ per thread), which the aligned
+// form (bar.sync) does not allow.
 __device__ __forceinline__ void named_sync(int id, int threads) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+  asm volatile("barrier.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 
 // Move slot `from` into slot `to` (shared state by lane 0, workspace fields by

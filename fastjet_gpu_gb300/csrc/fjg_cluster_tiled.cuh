@@ -29,14 +29,15 @@
 // at every step.  Each candidate set must be exactly the window, so that a
 // change of one pseudojet is seen by every slot whose neighbour it can be.
 //
-// Tile lists.  Per tile, a list of member slots with kTileSlack free entries
+// Tile lists.  Per tile, a list of member slots with S.slack free entries
 // after the live ones.  Removal writes a tombstone (-1) in place; a new jet
 // that changes tile is appended.  A reader running concurrently with these
 // updates sees either the old or the new word of any entry, and every reader
 // skips the slots involved in the merge by name, so no reader needs the
 // update to be finished.  The lists are rebuilt (tombstones squeezed out,
-// slack restored) every kTileSlack steps; at most one entry is appended per
-// step.
+// slack restored) every S.slack steps; at most one entry is appended per
+// step.  The slack is what the list area spares per tile (kListSlack entries
+// per possible tile, spread over the tiles in use), at most kTileSlackMax.
 //
 // Per step (T = 256 threads, 8 warps):
 //   S1  argmin over the tile summaries (smallest klo, its slot and khi,
@@ -58,7 +59,8 @@
 namespace fjg {
 
 constexpr int kTiledT = 256;
-constexpr int kTileSlack = 64;
+constexpr int kListSlack = 64;      // spare list entries per possible tile
+constexpr int kTileSlackMax = 256;  // rebuild interval bound (steps)
 constexpr int kMaxTiles = 4096;
 constexpr int kMaxWindowTiles = 9;
 constexpr int kMaxListed = 4 * kMaxTargets;  // targets recorded in S2
@@ -67,13 +69,70 @@ constexpr int kLargeWsBytesPerParticle = 96;  // bound of large_ws_bytes(N) / N 
 
 // Summary of one tile: the smallest key lower bound among its members, the
 // member holding it (lowest slot among equal bounds) with its key upper
-// bound, and the second smallest lower bound.
+// bound and neighbour field (neighbour, kind in the top bit), and the second
+// smallest lower bound without that member's mutual partner (see Cand).
 struct alignas(16) TileSum {
   float m1;
   int slot;
   float u1;
   float m2;
+  int nnk;
+  int pad0, pad1, pad2;
 };
+
+constexpr int kNoNeighbour = 0x7fffffff;    // neighbour field without a neighbour
+constexpr unsigned kPairBit = 0x80000000u;  // kind bit of the neighbour field: pair, not beam
+
+// Partial argmin of the keys for the certificate.  m2 is the smallest lower
+// bound among the other candidates, leaving out the best one's mutual
+// partner: two slots that are each other's neighbour with pair keys hold the
+// same exact key (the same FP64 expression of the same pair), and whichever
+// of them wins, the step merges that pair, so their tie needs no FP64
+// resolution.
+struct Cand {
+  float m1;  // smallest key lower bound
+  int slot;  // its slot (the lowest among equal bounds), -1 if none
+  float u1;  // its key upper bound
+  int nnk;   // its neighbour field
+  float m2;  // smallest lower bound of the others, without the mutual partner
+};
+
+__device__ __forceinline__ Cand cand_empty() {
+  return Cand{__int_as_float(0x7f800000), -1, __int_as_float(0x7f800000), kNoNeighbour, __int_as_float(0x7f800000)};
+}
+
+__device__ __forceinline__ bool cand_partners(int slot_x, int nnk_x, int slot_y, int nnk_y) {
+  return slot_x >= 0 && slot_y >= 0 && nnk_x == (int)((unsigned)slot_y | kPairBit) &&
+         nnk_y == (int)((unsigned)slot_x | kPairBit);
+}
+
+// x <- the combination of partials x and y.
+__device__ __forceinline__ void cand_merge(Cand& x, const Cand& y) {
+  if (y.m1 < x.m1 || (y.m1 == x.m1 && (unsigned)y.slot < (unsigned)x.slot)) {
+    const float cx = cand_partners(x.slot, x.nnk, y.slot, y.nnk) ? x.m2 : x.m1;
+    x = Cand{y.m1, y.slot, y.u1, y.nnk, fminf(y.m2, cx)};
+  } else {
+    x.m2 = fminf(x.m2, cand_partners(y.slot, y.nnk, x.slot, x.nnk) ? y.m2 : y.m1);
+  }
+}
+
+// Combination over a warp (every lane receives it).
+__device__ __forceinline__ Cand cand_warp(const Cand& c) {
+  const int lane = threadIdx.x & 31;
+  const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(c.m1));
+  const bool at_min = __float_as_uint(c.m1) == mb && c.slot >= 0;
+  const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)c.slot : 0xffffffffu);
+  const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)c.slot == sb);
+  const int src = ball ? __ffs(ball) - 1 : 0;
+  Cand r;
+  r.m1 = __uint_as_float(mb);
+  r.slot = ball ? (int)sb : -1;
+  r.u1 = __shfl_sync(kFull, c.u1, src);
+  r.nnk = __shfl_sync(kFull, c.nnk, src);
+  const float contrib = (ball && lane == src) ? c.m2 : (cand_partners(c.slot, c.nnk, r.slot, r.nnk) ? c.m2 : c.m1);
+  r.m2 = __uint_as_float(__reduce_min_sync(kFull, __float_as_uint(contrib)));
+  return r;
+}
 
 // Per-event large workspace: pointers into the event's region of
 // large_ws_bytes(N) bytes.
@@ -81,10 +140,11 @@ struct LargeWs {
   float *rap32, *phi32, *wlo, *whi, *nlo, *nhi, *klo, *khi;  // [N]
   int *nn, *tile, *pos;                                       // [N]
   int8_t *pair, *alive;                                       // [N]
-  int* members;                                               // [N + kTileSlack * MT]
+  int* members;                                               // [N + kListSlack * MT]
   int *t_start, *t_count;                                     // [MT]
   TileSum* tsum;                                              // [MT]
   int max_tiles;                                              // MT
+  int list_cap;                                               // bound of one tile's list length
 };
 
 __host__ __device__ __forceinline__ int large_max_tiles(int N) { return (N / 8 < kMaxTiles) ? N / 8 : kMaxTiles; }
@@ -92,7 +152,7 @@ __host__ __device__ __forceinline__ int large_max_tiles(int N) { return (N / 8 <
 __host__ __device__ __forceinline__ int64_t large_ws_bytes(int N) {
   const int64_t MT = large_max_tiles(N);
   const int64_t head = 8 * 4 * (int64_t)N + 3 * 4 * (int64_t)N + ((2 * (int64_t)N + 15) & ~(int64_t)15);
-  return head + 4 * ((int64_t)N + kTileSlack * MT) + 2 * 4 * MT + 16 + 16 * MT;
+  return head + 4 * ((int64_t)N + kListSlack * MT) + 2 * 4 * MT + 16 + 32 * MT;
 }
 
 __device__ __forceinline__ LargeWs large_ws(unsigned char* base, int N) {
@@ -116,20 +176,21 @@ __device__ __forceinline__ LargeWs large_ws(unsigned char* base, int N) {
   L.alive = b + N;
   int* m = reinterpret_cast<int*>(b + ((2 * N + 15) & ~15));
   L.members = m;
-  L.t_start = m + N + kTileSlack * MT;
+  L.t_start = m + N + kListSlack * MT;
   L.t_count = L.t_start + MT;
   const uintptr_t ts = (reinterpret_cast<uintptr_t>(L.t_count + MT) + 15) & ~uintptr_t(15);
   L.tsum = reinterpret_cast<TileSum*>(ts);
   L.max_tiles = MT;
+  L.list_cap = N + kTileSlackMax;
   return L;
 }
 
 struct TiledShared {
   static constexpr int W = kTiledT / 32;
   double rmin, inv_side_r, inv_side_phi;
-  int nrap, nphi, nt;
+  int nrap, nphi, nt, slack;
   int ta_u, ta_v;  // tile of the new jet (rapidity and azimuth index)
-  Cert warg[W];
+  Cand wcand[W];
   Arg wexact[W];
   Cert wcert[W];
   Cert rcert[kMaxTargets][W];
@@ -196,6 +257,35 @@ __device__ __forceinline__ bool tiles_adjacent(const TiledShared& S, int t1, int
   return dv <= 1 || dv == S.nphi - 1;
 }
 
+// Window scans.  The start and length of every tile of a window are read up
+// front (independent loads), then the members are visited in passes: in a
+// pass a thread takes the member at the same index of every tile, so that the
+// loads for one member of each tile are in flight together.  A length is
+// clamped to what a list can hold, so no scan is longer than the list area.
+// Each thread reads the lengths itself: a list that grows meanwhile (an
+// append in S3a) only adds or drops its last member, the new jet, which every
+// caller skips by name.
+template <int NT>
+struct TileRanges {
+  int start[NT], len[NT], tile[NT];
+  int maxlen;
+};
+
+template <int NT>
+__device__ __forceinline__ TileRanges<NT> tile_ranges(const LargeWs& L, const int* tiles, int nw) {
+  TileRanges<NT> r;
+  r.maxlen = 0;
+#pragma unroll
+  for (int k = 0; k < NT; ++k) {
+    r.tile[k] = k < nw ? tiles[k] : 0;
+    r.start[k] = k < nw ? L.t_start[r.tile[k]] : 0;
+    const int m = k < nw ? L.t_count[r.tile[k]] : 0;
+    r.len[k] = min(max(m, 0), L.list_cap);
+    r.maxlen = max(r.maxlen, r.len[k]);
+  }
+  return r;
+}
+
 __device__ __forceinline__ double dr2_ws(const Ws& g, int s, int t) {
   return dr2_64(g.at(kRap, s), g.at(kPhi, s), g.at(kRap, t), g.at(kPhi, t));
 }
@@ -240,15 +330,25 @@ __device__ __forceinline__ void window_cert(const TiledShared& S, const LargeWs&
   int tiles[kMaxWindowTiles];
   const int nw = window_tiles(S, L.tile[t], tiles);
   const float rt = L.rap32[t], pt = L.phi32[t];
-  for (int k = 0; k < nw; ++k) {
-    const int tt = tiles[k];
-    const int base = L.t_start[tt], m = L.t_count[tt];
-    for (int i = first; i < m; i += nthreads) {
-      const int u = L.members[base + i];
-      if (u < 0 || u == t || u == skip1 || u == skip2) continue;
+  const TileRanges<kMaxWindowTiles> R = tile_ranges<kMaxWindowTiles>(L, tiles, nw);
+  for (int i = first; i < R.maxlen; i += nthreads) {
+    int u[kMaxWindowTiles];
+    float r[kMaxWindowTiles], ph[kMaxWindowTiles];
+#pragma unroll
+    for (int k = 0; k < kMaxWindowTiles; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
+#pragma unroll
+    for (int k = 0; k < kMaxWindowTiles; ++k) {
+      if (u[k] >= 0) {
+        r[k] = L.rap32[u[k]];
+        ph[k] = L.phi32[u[k]];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxWindowTiles; ++k) {
+      if (u[k] < 0 || u[k] == t || u[k] == skip1 || u[k] == skip2) continue;
       float lo, hi;
-      dr2_32(rt, pt, L.rap32[u], L.phi32[u], X.bd, lo, hi);
-      cert_add(c, lo, hi, u);
+      dr2_32(rt, pt, r[k], ph[k], X.bd, lo, hi);
+      cert_add(c, lo, hi, u[k]);
     }
   }
 }
@@ -301,36 +401,34 @@ __device__ __forceinline__ int resolve_large(const TiledShared& S, const LargeWs
   return r.idx;
 }
 
-// Summary of tile tt (whole warp).
+// Summary of tile tt (whole warp).  A member's neighbour field is read only
+// when it becomes a lane's best or may be its best's mutual partner.
 __device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
   const int lane = threadIdx.x & 31;
-  Cert c = cert_empty();
+  Cand c = cand_empty();
   const int base = L.t_start[tt], m = L.t_count[tt];
   for (int i = lane; i < m; i += 32) {
     const int u = L.members[base + i];
     if (u < 0) continue;
     const float lo = L.klo[u];
-    if (lo < c.m1 || (lo == c.m1 && (unsigned)u < (unsigned)c.i1)) {
-      c.m2 = c.m1;
-      c.m1 = lo;
-      c.u1 = L.khi[u];
-      c.i1 = u;
+    if (lo < c.m1 || (lo == c.m1 && (unsigned)u < (unsigned)c.slot)) {
+      const int unnk = (L.nn[u] < 0 ? kNoNeighbour : L.nn[u]) | (L.pair[u] ? (int)kPairBit : 0);
+      const float cx = cand_partners(c.slot, c.nnk, u, unnk) ? c.m2 : c.m1;
+      c = Cand{lo, u, L.khi[u], unnk, cx};
     } else {
-      c.m2 = fminf(c.m2, lo);
+      bool partners = false;
+      if (c.nnk == (int)((unsigned)u | kPairBit)) {
+        const int unnk = (L.nn[u] < 0 ? kNoNeighbour : L.nn[u]) | (L.pair[u] ? (int)kPairBit : 0);
+        partners = cand_partners(u, unnk, c.slot, c.nnk);
+      }
+      if (!partners) c.m2 = fminf(c.m2, lo);
     }
   }
-  const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(c.m1));
-  const bool at_min = __float_as_uint(c.m1) == mb && c.i1 >= 0;
-  const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)c.i1 : 0xffffffffu);
-  const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)c.i1 == sb);
-  const int src = ball ? __ffs(ball) - 1 : 0;
-  const float u1 = __shfl_sync(kFull, c.u1, src);
-  const unsigned other = (ball && lane == src) ? __float_as_uint(c.m2) : __float_as_uint(c.m1);
-  const float m2 = __uint_as_float(__reduce_min_sync(kFull, other));
-  if (lane == 0) L.tsum[tt] = TileSum{__uint_as_float(mb), ball ? (int)sb : -1, u1, m2};
+  const Cand w = cand_warp(c);
+  if (lane == 0) L.tsum[tt] = TileSum{w.m1, w.slot, w.u1, w.m2, w.nnk, 0, 0, 0};
 }
 
-// Block-wide rebuild of the tile lists from the live slots (kTileSlack free
+// Block-wide rebuild of the tile lists from the live slots (S.slack free
 // entries per tile, filled with tombstones) and of every tile summary.
 __device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N) {
   constexpr int W = kTiledT / 32;
@@ -344,7 +442,7 @@ __device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N) {
   int carry = 0;
   for (int base = 0; base < S.nt; base += kTiledT) {
     const int t = base + tid;
-    const int v = (t < S.nt) ? L.t_count[t] + kTileSlack : 0;
+    const int v = (t < S.nt) ? L.t_count[t] + S.slack : 0;
     int incl = v;
     for (int o = 1; o < 32; o <<= 1) {
       const int x = __shfl_up_sync(kFull, incl, o);
@@ -374,7 +472,7 @@ __device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N) {
   __syncthreads();
   for (int t = warp; t < S.nt; t += W) {
     const int end = L.t_start[t] + L.t_count[t];
-    for (int i = lane; i < kTileSlack; i += 32) L.members[end + i] = -1;
+    for (int i = lane; i < S.slack; i += 32) L.members[end + i] = -1;
   }
   __syncthreads();
   for (int t = warp; t < S.nt; t += W) tile_summary(L, t);
@@ -489,6 +587,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     S.nrap = nrap;
     S.nphi = nphi;
     S.nt = nrap * nphi;
+    S.slack = min(kTileSlackMax, kListSlack * L.max_tiles / S.nt);
     S.rmin = lo;
     S.inv_side_r = (double)nrap / fmax(hi - lo, side_min);
     S.inv_side_phi = (double)nphi / 6.283185307179586;
@@ -553,48 +652,24 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   int n = N;
   int step = 0;
   while (n > 0) {
-    if (step > 0 && step % kTileSlack == 0) rebuild_tiles(S, L, N);
+    if (step > 0 && step % S.slack == 0) rebuild_tiles(S, L, N);
 
     // S1: argmin over the tile summaries (slot order breaks ties)
-    Cert mine = cert_empty();
+    Cand mine = cand_empty();
     for (int t = tid; t < S.nt; t += T) {
       const TileSum ts = L.tsum[t];
-      if (ts.m1 < mine.m1 || (ts.m1 == mine.m1 && (unsigned)ts.slot < (unsigned)mine.i1)) {
-        mine.m2 = fminf(mine.m1, ts.m2);
-        mine.m1 = ts.m1;
-        mine.u1 = ts.u1;
-        mine.i1 = ts.slot;
-      } else {
-        mine.m2 = fminf(mine.m2, ts.m1);
-      }
+      cand_merge(mine, Cand{ts.m1, ts.slot, ts.u1, ts.nnk, ts.m2});
     }
     {
-      const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(mine.m1));
-      const bool at_min = __float_as_uint(mine.m1) == mb && mine.i1 >= 0;
-      const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)mine.i1 : 0xffffffffu);
-      const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)mine.i1 == sb);
-      const int src = ball ? __ffs(ball) - 1 : 0;
-      Cert wc;
-      wc.m1 = __uint_as_float(mb);
-      wc.i1 = ball ? (int)sb : -1;
-      wc.u1 = __shfl_sync(kFull, mine.u1, src);
-      const unsigned other = (ball && lane == src) ? __float_as_uint(mine.m2) : __float_as_uint(mine.m1);
-      wc.m2 = __uint_as_float(__reduce_min_sync(kFull, other));
-      if (lane == 0) S.warg[warp] = wc;
+      const Cand wc = cand_warp(mine);
+      if (lane == 0) S.wcand[warp] = wc;
     }
     __syncthreads();  // B1
     int c;
     {
-      const Cert x = (lane < W) ? S.warg[lane] : cert_empty();
-      const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(x.m1));
-      const bool at_min = __float_as_uint(x.m1) == mb && x.i1 >= 0;
-      const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)x.i1 : 0xffffffffu);
-      const unsigned ball = __ballot_sync(kFull, at_min && (unsigned)x.i1 == sb);
-      const int src = ball ? __ffs(ball) - 1 : 0;
-      c = ball ? (int)sb : -1;
-      const float u1 = __shfl_sync(kFull, x.u1, src);
-      const unsigned other = (ball && lane == src) ? __float_as_uint(x.m2) : __float_as_uint(x.m1);
-      const float m2 = __uint_as_float(__reduce_min_sync(kFull, other));
+      const Cand x = cand_warp((lane < W) ? S.wcand[lane] : cand_empty());
+      c = x.slot;
+      const float u1 = x.u1, m2 = x.m2;
       if (c >= 0 && !(u1 < m2)) {
         // near-tie: exact keys of every slot whose lower bound is <= u1
         unsigned long long bk = ~0ull;
@@ -703,15 +778,20 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       const int r0 = tid - 32 * MW;
       int tiles[2 * kMaxWindowTiles];
       const int nw = window_union(S, tile_c, tile_j, tiles);
-      for (int k = 0; k < nw; ++k) {
-        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
-        for (int i = r0; i < m; i += TR) {
-          const int u = L.members[base + i];
-          if (u < 0 || u == c || u == j) continue;
-          const int nu = L.nn[u];
-          if (nu == c || (pair && nu == j)) {
+      constexpr int NU = 2 * kMaxWindowTiles;
+      const TileRanges<NU> R = tile_ranges<NU>(L, tiles, nw);
+      for (int i = r0; i < R.maxlen; i += TR) {
+        int u[NU], nu[NU];
+#pragma unroll
+        for (int k = 0; k < NU; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
+#pragma unroll
+        for (int k = 0; k < NU; ++k) nu[k] = u[k] >= 0 ? L.nn[u[k]] : -1;
+#pragma unroll
+        for (int k = 0; k < NU; ++k) {
+          if (u[k] < 0 || u[k] == c || u[k] == j) continue;
+          if (nu[k] == c || (pair && nu[k] == j)) {
             const int p = atomicAdd(&S.n_rescan, 1);
-            if (p < kMaxListed) S.rlist[p] = u;
+            if (p < kMaxListed) S.rlist[p] = u[k];
           }
         }
       }
@@ -808,26 +888,41 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       int tiles[kMaxWindowTiles];
       const int nw = window_tiles(S, ta, tiles);
       const float ra = L.rap32[a], pa = L.phi32[a];
-      for (int k = 0; k < nw; ++k) {
-        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
-        for (int i = tid; i < m; i += T) {
-          const int t = L.members[base + i];
+      constexpr int NT = kMaxWindowTiles;
+      const TileRanges<NT> R = tile_ranges<NT>(L, tiles, nw);
+      for (int i = tid; i < R.maxlen; i += T) {
+        int u[NT], cn[NT];
+        float r[NT], ph[NT], nl[NT], nh[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+          if (u[k] >= 0) {
+            r[k] = L.rap32[u[k]];
+            ph[k] = L.phi32[u[k]];
+            cn[k] = L.nn[u[k]];
+            nl[k] = L.nlo[u[k]];
+            nh[k] = L.nhi[u[k]];
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+          const int t = u[k];
           if (t < 0 || t == a || t == b) continue;
           float lo, hi;
-          dr2_32(L.rap32[t], L.phi32[t], ra, pa, X.bd, lo, hi);
+          dr2_32(r[k], ph[k], ra, pa, X.bd, lo, hi);
           cert_add(ca, lo, hi, t);
-          const int cn = L.nn[t];
-          if (cn == a) continue;
+          if (cn[k] == a) continue;
           bool closer;
           float ulo = lo, uhi = hi;
-          if (cn < 0 || hi < L.nlo[t]) {
+          if (cn[k] < 0 || hi < nl[k]) {
             closer = true;
-          } else if (lo > L.nhi[t]) {
+          } else if (lo > nh[k]) {
             closer = false;
           } else {
             const double da = dr2_ws(g, t, a);
-            const double dc = dr2_ws(g, t, cn);
-            closer = da < dc || (da == dc && a < cn);
+            const double dc = dr2_ws(g, t, cn[k]);
+            closer = da < dc || (da == dc && a < cn[k]);
             ulo = fjk_to_f32(da, 1);
             uhi = fjk_to_f32(da, 2);
           }
@@ -836,7 +931,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
             L.nlo[t] = ulo;
             L.nhi[t] = uhi;
             set_key_large(L, X, t);
-            mark_dirty(S, tiles[k]);
+            mark_dirty(S, R.tile[k]);
           }
         }
       }

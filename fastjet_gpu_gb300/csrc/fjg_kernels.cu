@@ -5,7 +5,7 @@
 namespace fjg {
 
 // Persistent tiled kernel for events above kSmemMaxN particles.
-__global__ void __launch_bounds__(kTiledT) k_cluster_tiled(BatchArgs A) {
+__global__ void __launch_bounds__(kTiledT, 1) k_cluster_tiled(BatchArgs A) {
   __shared__ TiledShared S;
   const int count = *A.n_order;
   for (;;) {
