@@ -322,6 +322,22 @@ __device__ __forceinline__ double exact_key_large(const LargeWs& L, const EventC
   return pair_distance(X.g.at(kW, t), X.g.at(kW, nn), dr2_ws(X.g, t, nn), X.inv_r2);
 }
 
+// Bounds of dR2(t, u) from the FP32 filter's [lo, hi]; when that interval is
+// wide (close pairs: the filter's error is absolute) the FP64 value is taken
+// instead, so that the key intervals built on it stay narrow and the argmin
+// certificates rarely fail.
+__device__ __forceinline__ void tight_dr2(const EventCtx& X, int t, int u, float lo, float hi, float& lo_out,
+                                          float& hi_out) {
+  if (hi - lo <= lo * 0x1p-16f) {
+    lo_out = lo;
+    hi_out = hi;
+  } else {
+    const double d = dr2_ws(X.g, t, u);
+    lo_out = fjk_to_f32(d, 1);
+    hi_out = fjk_to_f32(d, 2);
+  }
+}
+
 // Certificate partial of slot t's nearest neighbour over the window of its
 // tile, visited by `nthreads` threads starting at `first`; slots t, skip1 and
 // skip2 and tombstones are skipped.
@@ -364,8 +380,7 @@ __device__ __forceinline__ int resolve_large(const TiledShared& S, const LargeWs
     return -1;
   }
   if (cert_ok(c)) {
-    lo_out = c.m1;
-    hi_out = c.u1;
+    tight_dr2(X, t, c.i1, c.m1, c.u1, lo_out, hi_out);
     return c.i1;
   }
   const int lane = threadIdx.x & 31;
@@ -401,36 +416,65 @@ __device__ __forceinline__ int resolve_large(const TiledShared& S, const LargeWs
   return r.idx;
 }
 
-// Summary of tile tt (whole warp).  A member's neighbour field is read only
-// when it becomes a lane's best or may be its best's mutual partner.
+// Summary of tile tt (whole warp).  Each lane keeps its two smallest lower
+// bounds with their slots and the third smallest bound, reading four members
+// per pass; the winner's neighbour field (and its neighbour's, to recognise
+// a mutual partner) is read once at the end.
 __device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
+  constexpr int B = 4;
   const int lane = threadIdx.x & 31;
-  Cand c = cand_empty();
-  const int base = L.t_start[tt], m = L.t_count[tt];
-  for (int i = lane; i < m; i += 32) {
-    const int u = L.members[base + i];
-    if (u < 0) continue;
-    const float lo = L.klo[u];
-    if (lo < c.m1 || (lo == c.m1 && (unsigned)u < (unsigned)c.slot)) {
-      const int unnk = (L.nn[u] < 0 ? kNoNeighbour : L.nn[u]) | (L.pair[u] ? (int)kPairBit : 0);
-      const float cx = cand_partners(c.slot, c.nnk, u, unnk) ? c.m2 : c.m1;
-      c = Cand{lo, u, L.khi[u], unnk, cx};
-    } else {
-      bool partners = false;
-      if (c.nnk == (int)((unsigned)u | kPairBit)) {
-        const int unnk = (L.nn[u] < 0 ? kNoNeighbour : L.nn[u]) | (L.pair[u] ? (int)kPairBit : 0);
-        partners = cand_partners(u, unnk, c.slot, c.nnk);
+  const float inf = __int_as_float(0x7f800000);
+  float m1 = inf, m2 = inf, m3 = inf;
+  int s1 = -1, s2 = -1;
+  const int base = L.t_start[tt], m = min(max(L.t_count[tt], 0), L.list_cap);
+  for (int i0 = lane; i0 < m; i0 += 32 * B) {
+    int u[B];
+    float lo[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) u[q] = i0 + 32 * q < m ? L.members[base + i0 + 32 * q] : -1;
+#pragma unroll
+    for (int q = 0; q < B; ++q) lo[q] = u[q] >= 0 ? L.klo[u[q]] : inf;
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      if (u[q] < 0) continue;
+      if (lo[q] < m1 || (lo[q] == m1 && (unsigned)u[q] < (unsigned)s1)) {
+        m3 = m2;
+        m2 = m1;
+        s2 = s1;
+        m1 = lo[q];
+        s1 = u[q];
+      } else if (lo[q] < m2 || (lo[q] == m2 && (unsigned)u[q] < (unsigned)s2)) {
+        m3 = m2;
+        m2 = lo[q];
+        s2 = u[q];
+      } else {
+        m3 = fminf(m3, lo[q]);
       }
-      if (!partners) c.m2 = fminf(c.m2, lo);
     }
   }
-  const Cand w = cand_warp(c);
-  if (lane == 0) L.tsum[tt] = TileSum{w.m1, w.slot, w.u1, w.m2, w.nnk, 0, 0, 0};
+  const unsigned mb = __reduce_min_sync(kFull, __float_as_uint(m1));
+  const bool at_min = __float_as_uint(m1) == mb && s1 >= 0;
+  const unsigned sb = __reduce_min_sync(kFull, at_min ? (unsigned)s1 : 0xffffffffu);
+  const int x = sb == 0xffffffffu ? -1 : (int)sb;
+  int nnk = kNoNeighbour, p = -1;
+  float u1 = inf;
+  if (lane == 0 && x >= 0) {
+    const int nx = L.nn[x];
+    const bool px = L.pair[x] != 0;
+    u1 = L.khi[x];
+    nnk = (nx < 0 ? kNoNeighbour : nx) | (px ? (int)kPairBit : 0);
+    if (px && nx >= 0 && L.pair[nx] != 0 && L.nn[nx] == x) p = nx;
+  }
+  p = __shfl_sync(kFull, p, 0);
+  // smallest bound of the lane's members other than the winner and its partner
+  const float contrib = (s1 >= 0 && s1 != x && s1 != p) ? m1 : (s2 >= 0 && s2 != x && s2 != p) ? m2 : m3;
+  const float mo = __uint_as_float(__reduce_min_sync(kFull, __float_as_uint(contrib)));
+  if (lane == 0) L.tsum[tt] = TileSum{__uint_as_float(mb), x, u1, mo, nnk, 0, 0, 0};
 }
 
 // Block-wide rebuild of the tile lists from the live slots (S.slack free
 // entries per tile, filled with tombstones) and of every tile summary.
-__device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N) {
+__device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N, bool summaries = true) {
   constexpr int W = kTiledT / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int t = tid; t < S.nt; t += kTiledT) L.t_count[t] = 0;
@@ -475,8 +519,10 @@ __device__ inline void rebuild_tiles(TiledShared& S, const LargeWs& L, int N) {
     for (int i = lane; i < S.slack; i += 32) L.members[end + i] = -1;
   }
   __syncthreads();
-  for (int t = warp; t < S.nt; t += W) tile_summary(L, t);
-  __syncthreads();
+  if (summaries) {
+    for (int t = warp; t < S.nt; t += W) tile_summary(L, t);
+    __syncthreads();
+  }
 }
 
 __device__ __forceinline__ void mark_dirty(TiledShared& S, int t) {
@@ -603,7 +649,8 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   __syncthreads();
   for (int s = tid; s < N; s += T) L.tile[s] = tile_u(S, g.at(kRap, s)) * S.nphi + tile_v(S, g.at(kPhi, s));
   __syncthreads();
-  rebuild_tiles(S, L, N);  // (summaries are recomputed once the keys exist)
+  // lists only: the summaries read neighbours and keys, which do not exist yet
+  rebuild_tiles(S, L, N, false);
 
   // ---- initial nearest neighbours within the windows
   for (int t = tid; t < N; t += T) {
@@ -611,6 +658,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     window_cert(S, L, X, t, 0, 1, -1, -1, c);
     int nn = c.i1;
     float nlo = c.m1, nhi = c.u1;
+    if (nn >= 0 && cert_ok(c)) tight_dr2(X, t, nn, c.m1, c.u1, nlo, nhi);
     if (nn >= 0 && !cert_ok(c)) {
       unsigned long long bk = ~0ull;
       int bi = 0x7fffffff;
@@ -917,6 +965,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           float ulo = lo, uhi = hi;
           if (cn[k] < 0 || hi < nl[k]) {
             closer = true;
+            tight_dr2(X, t, a, lo, hi, ulo, uhi);
           } else if (lo > nh[k]) {
             closer = false;
           } else {
