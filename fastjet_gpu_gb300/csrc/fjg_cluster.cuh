@@ -1,13 +1,15 @@
 // Clustering of one event per CTA (sm_103a), decision state in shared memory.
 //
 // Each CTA runs a persistent loop over a list of events.  Per slot (pseudojet):
-//   shared memory (what every step reads; 45 bytes a slot, so several CTAs
+//   shared memory (what every step reads; 36 bytes a slot, so several CTAs
 //   share an SM and hide each other's serial latency):
 //     FP32  rap32, phi32                  filter coordinates
-//     FP32  wlo/whi, nlo/nhi, klo/khi     intervals bracketing the exact FP64
+//     FP32  wlo (+ int8 wx), nlo/nhi, klo/khi
+//                                         intervals bracketing the exact FP64
 //                                         weight, dR2 to the nearest neighbour,
 //                                         and key
-//     int32 nn (slot of the nearest neighbour), label (lowest constituent index)
+//     int16 nn (slot of the nearest neighbour), label (lowest constituent
+//           index), rlist (rescan targets of a step)
 //     int8  pair (the key is the pair distance, not the beam distance)
 //   global workspace (L2-resident; read at merges and on the rare exact path):
 //     FP64  rap, phi, w, px, py, pz, E    exact values
@@ -96,15 +98,27 @@ __device__ __forceinline__ void signal_done(const BatchArgs& A, int e) {
 }
 
 constexpr int kRescanChunk = 8;  // targets per register pass
-constexpr int kMaxTargets = 32;  // targets per step scanned during the merge
+constexpr int kMaxTargets = 16;  // targets per step scanned during the merge
 
 template <int T, int SPT>
 struct SmemLayout {
   static constexpr int C = T * SPT;
   static constexpr int W = T / 32;
-  float rap32[C], phi32[C], wlo[C], whi[C], nlo[C], nhi[C], klo[C], khi[C];
-  int32_t nn[C], label[C], rlist[C];
-  int8_t pair[C];
+  // 36 B per slot, so that three CTAs of 2048 slots fit on an SM.  Slots,
+  // neighbours and labels are below 4096 (int16).  The weight interval is
+  // stored as its lower end and whether it is a single float (wx): the upper
+  // end of a directed-rounding pair is the next float up otherwise.
+  float rap32[C], phi32[C], wlo[C], nlo[C], nhi[C], klo[C], khi[C];
+  int16_t nn[C], label[C], rlist[C];
+  int8_t pair[C], wx[C];
+  __device__ __forceinline__ float whi(int t) const {
+    return wx[t] ? wlo[t] : __int_as_float(__float_as_int(wlo[t]) + 1);
+  }
+  __device__ __forceinline__ void set_w(int t, double w) {
+    const float lo = fjk_to_f32(w, 1);
+    wlo[t] = lo;
+    wx[t] = fjk_to_f32(w, 2) == lo;
+  }
   // reduction and control scratch
   Cert warg[W];
   int wlab[W], wnn[W], wpair[W];  // label, neighbour and kind of each warp's candidate
@@ -168,12 +182,12 @@ __device__ __forceinline__ void set_key(SmemLayout<T, SPT>& S, const EventCtx& X
   const int nn = S.nn[t];
   if (nn < 0) {
     S.klo[t] = S.wlo[t];
-    S.khi[t] = S.whi[t];
+    S.khi[t] = S.whi(t);
     S.pair[t] = 0;
     return;
   }
   float klo, khi;
-  const int kind = key_interval(S.wlo[t], S.whi[t], S.wlo[nn], S.whi[nn], S.nlo[t], S.nhi[t], X.ilo, X.ihi, klo, khi);
+  const int kind = key_interval(S.wlo[t], S.whi(t), S.wlo[nn], S.whi(nn), S.nlo[t], S.nhi[t], X.ilo, X.ihi, klo, khi);
   if (kind >= 0) {
     S.klo[t] = klo;
     S.khi[t] = khi;
@@ -314,7 +328,7 @@ __device__ __forceinline__ void move_slot_warp(SmemLayout<T, SPT>& S, const Ws& 
     S.rap32[to] = S.rap32[from];
     S.phi32[to] = S.phi32[from];
     S.wlo[to] = S.wlo[from];
-    S.whi[to] = S.whi[from];
+    S.wx[to] = S.wx[from];
     S.nlo[to] = S.nlo[from];
     S.nhi[to] = S.nhi[from];
     S.klo[to] = S.klo[from];
@@ -363,8 +377,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
     g.at(kW, s) = kin.w;
     S.rap32[s] = fjk_to_f32(kin.rap, 0);
     S.phi32[s] = fjk_to_f32(kin.phi, 0);
-    S.wlo[s] = fjk_to_f32(kin.w, 1);
-    S.whi[s] = fjk_to_f32(kin.w, 2);
+    S.set_w(s, kin.w);
     S.label[s] = s;
     rmax = fmax(rmax, fabs(kin.rap));
     if (A.owner) A.owner[off + s] = s;  // union-find parent by label
@@ -622,8 +635,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
         if (lane == 0 && w_role) {
           const double w = fjk_weight(px, py, X.algo);
           g.at(kW, a) = w;
-          S.wlo[a] = fjk_to_f32(w, 1);
-          S.whi[a] = fjk_to_f32(w, 2);
+          S.set_w(a, w);
           const double d = pair_distance(wc, wj, dr2_64(rc, fc, rj, fj), X.inv_r2);
           if (A.history) A.history[off + step] = StepRec{lo_l, hi_l, d};
           if (A.owner) A.owner[off + hi_l] = lo_l;

@@ -21,9 +21,26 @@ __global__ void __launch_bounds__(kTiledT, 1) k_cluster_tiled(BatchArgs A) {
   }
 }
 
+int launch_priority(int level) {
+  static int range[64][3] = {};  // resolved, least, greatest
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int least = 0, greatest = 0;
+  if (dev >= 0 && dev < 64 && range[dev][0]) {
+    least = range[dev][1];
+    greatest = range[dev][2];
+  } else if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess && dev >= 0 && dev < 64) {
+    range[dev][0] = 1;
+    range[dev][1] = least;
+    range[dev][2] = greatest;
+  }
+  // numerically lower is more urgent: greatest <= least
+  const int p = greatest + level;
+  return p > least ? least : p;
+}
+
 cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
-  k_cluster_tiled<<<grid < 1 ? 1 : grid, kTiledT, 0, s>>>(A);
-  return cudaGetLastError();
+  return launch_with_priority(k_cluster_tiled, grid, kTiledT, 0, s, 0, A);
 }
 
 // Events are handed to the bucket kernels largest first (longest-processing-
@@ -191,33 +208,45 @@ bool tuning_valid(const Tuning& t) {
   return t.large_ctas_per_sm >= 1 && t.large_ctas_per_sm <= 8 && t.tile_factor >= 1.0 && t.tile_factor <= 8.0;
 }
 
-cudaError_t launch_variant(int v, const BatchArgs& A, int grid, cudaStream_t s) {
-  cudaError_t err = launch_variant_small(v, A, grid, s);
-  if (err == cudaErrorInvalidValue) err = launch_variant_large(v, A, grid, s);
-  return err;
-}
-
-int variant_occupancy(int v) {
-  static int cache[64][kNumVariants] = {};
+static int occupancy_cached(int v, bool capped) {
+  static int cache[64][kNumVariants][2] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  int* slot = (dev >= 0 && dev < 64 && v >= 0 && v < kNumVariants) ? &cache[dev][v] : nullptr;
+  int* slot = (dev >= 0 && dev < 64 && v >= 0 && v < kNumVariants) ? &cache[dev][v][capped ? 1 : 0] : nullptr;
   if (slot && *slot > 0) return *slot;
-  int nb = occupancy_variant_small(v);
-  if (nb < 0) nb = occupancy_variant_large(v);
+  int nb = occupancy_variant_small(v, capped);
+  if (nb < 0) nb = occupancy_variant_large(v, capped);
   if (nb < 1) nb = 1;
   if (slot) *slot = nb;
   return nb;
 }
 
-// Persistent grid of bucket b: the configured CTAs per SM, at most what fits,
-// at most one CTA per event.
-static int bucket_grid(const Tuning& tune, int b, int num_sms, int n_events) {
+int variant_occupancy_plain(int v) { return occupancy_cached(v, false); }
+
+int variant_occupancy(int v) {
+  const int plain = occupancy_cached(v, false), capped = occupancy_cached(v, true);
+  return plain > capped ? plain : capped;
+}
+
+cudaError_t launch_variant(int v, const BatchArgs& A, int grid, int per_sm, cudaStream_t s) {
+  const bool capped = per_sm > variant_occupancy_plain(v);
+  cudaError_t err = launch_variant_small(v, A, grid, capped, s);
+  if (err == cudaErrorInvalidValue) err = launch_variant_large(v, A, grid, capped, s);
+  return err;
+}
+
+// Persistent grid of bucket b: the configured CTAs per SM (0: as many as the
+// plain build fits), at most what any build fits, at most one CTA per event.
+int bucket_per_sm(const Tuning& tune, int b) {
   const int v = tune.bucket[b].variant;
+  const int per_sm = tune.bucket[b].ctas_per_sm;
+  if (per_sm <= 0) return variant_occupancy_plain(v);
   const int fit = variant_occupancy(v);
-  int per_sm = tune.bucket[b].ctas_per_sm;
-  if (per_sm <= 0 || per_sm > fit) per_sm = fit;
-  int grid = num_sms * per_sm;
+  return per_sm > fit ? fit : per_sm;
+}
+
+static int bucket_grid(const Tuning& tune, int b, int num_sms, int n_events) {
+  int grid = num_sms * bucket_per_sm(tune, b);
   if (grid > n_events) grid = n_events;
   return grid < 1 ? 1 : grid;
 }
@@ -246,8 +275,8 @@ cudaError_t launch_batch(const BatchArgs& base, const Scratch& sc, int n_events,
     A.queue = sc.queues + b;
     A.ws = sc.ws;
     A.ws_stride = sc.ws_stride;
-    if ((err = launch_variant(tune.bucket[b].variant, A, bucket_grid(tune, b, num_sms, n_events), s)) !=
-        cudaSuccess)
+    if ((err = launch_variant(tune.bucket[b].variant, A, bucket_grid(tune, b, num_sms, n_events),
+                              bucket_per_sm(tune, b), s)) != cudaSuccess)
       return err;
     if (side) {
       if ((err = cudaEventRecord(ev_join[b], s)) != cudaSuccess) return err;
@@ -269,8 +298,8 @@ cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int
     A.queue = sc.queues + b;
     A.ws = sc.ws;
     A.ws_stride = sc.ws_stride;
-    if ((err = launch_variant(tune.bucket[b].variant, A, bucket_grid(tune, b, num_sms, n_events), stream)) !=
-        cudaSuccess)
+    if ((err = launch_variant(tune.bucket[b].variant, A, bucket_grid(tune, b, num_sms, n_events),
+                              bucket_per_sm(tune, b), stream)) != cudaSuccess)
       return err;
   }
   return cudaSuccess;
@@ -305,7 +334,7 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, const
     k_cluster_tiled<<<1, kTiledT, 0, stream>>>(A);
     return cudaGetLastError();
   }
-  return launch_variant(tune.bucket[b].variant, A, 1, stream);
+  return launch_variant(tune.bucket[b].variant, A, 1, 1, stream);
 }
 
 __global__ void k_kinematics(const double* p4, int n, int algo, double* rap, double* phi, double* w) {

@@ -66,13 +66,41 @@ struct Tuning {
 inline Tuning default_tuning() { return Tuning{{{0, 0}, {2, 0}, {5, 0}, {7, 0}, {9, 0}}, 2, 1.0}; }
 bool tuning_valid(const Tuning& t);
 
+// Scheduling priority of a clustering launch: level 0 (the tiled kernel) is
+// the most urgent, then the size buckets from the largest down
+// (level kNumBuckets - b), so that when the bucket kernels of one batch run
+// side by side the SMs take the longest events first and the small buckets
+// fill the tail.  Levels beyond the device's range share its lowest priority.
+int launch_priority(int level);
+inline int bucket_priority_level(int b) { return kNumBuckets - b; }
+
+// Launch of a clustering kernel with its priority as a launch attribute
+// (recorded in a captured graph too).
+template <class K>
+cudaError_t launch_with_priority(K kernel, int grid, int threads, size_t smem, cudaStream_t s, int level,
+                                 const BatchArgs& A) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid < 1 ? 1 : grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = launch_priority(level);
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, A);
+}
+
 // The tiled kernel over the work list of A (a persistent grid of `grid` CTAs).
 cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s);
 
 // Launch variant v (a persistent grid of `grid` CTAs); resident CTAs per SM of
 // variant v on the current device.
-cudaError_t launch_variant(int v, const BatchArgs& A, int grid, cudaStream_t s);
-int variant_occupancy(int v);
+cudaError_t launch_variant(int v, const BatchArgs& A, int grid, int per_sm, cudaStream_t s);
+int variant_occupancy(int v);        // most CTAs per SM of any build of variant v
+int variant_occupancy_plain(int v);  // of its plain build (more takes the register-capped one)
+int bucket_per_sm(const Tuning& tune, int b);  // CTAs per SM that bucket b runs with
 
 // Device-side batch descriptor scratch owned by a context.
 struct Scratch {

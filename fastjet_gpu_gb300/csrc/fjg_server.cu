@@ -205,11 +205,8 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
     const int grid = std::min(m, ctx->num_sms * ctx->tune.large_ctas_per_sm);
     err = fjg::launch_tiled(A, grid, L.stream);
   } else {
-    const int v = ctx->tune.bucket[q].variant;
-    const int fit = fjg::variant_occupancy(v);
-    int per_sm = ctx->tune.bucket[q].ctas_per_sm;
-    if (per_sm <= 0 || per_sm > fit) per_sm = fit;
-    err = fjg::launch_variant(v, A, std::min(m, ctx->num_sms * per_sm), L.stream);
+    const int per_sm = fjg::bucket_per_sm(ctx->tune, q);
+    err = fjg::launch_variant(ctx->tune.bucket[q].variant, A, std::min(m, ctx->num_sms * per_sm), per_sm, L.stream);
   }
   if (err == cudaSuccess) err = cudaMemcpyAsync(L.h_status, L.d_status, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
   if (err == cudaSuccess) err = cudaEventRecord(L.ev, L.stream);
@@ -424,9 +421,7 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
   S->free_slots.reserve(c.max_inflight);
   for (int k = c.max_inflight - 1; k >= 0; --k) S->free_slots.push_back(k);
   for (int q = 0; q < fjg::kNumBuckets; ++q)
-    S->limit[q] = c.oversubscribe * ctx->num_sms *
-                  std::max(1, std::min(fjg::variant_occupancy(ctx->tune.bucket[q].variant),
-                                       ctx->tune.bucket[q].ctas_per_sm > 0 ? ctx->tune.bucket[q].ctas_per_sm : 64));
+    S->limit[q] = c.oversubscribe * ctx->num_sms * std::max(1, fjg::bucket_per_sm(ctx->tune, q));
   S->limit[fjg::kLargeQueue] = c.oversubscribe * ctx->num_sms * ctx->tune.large_ctas_per_sm;
   *out = S;
   return FJG_OK;

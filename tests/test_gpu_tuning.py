@@ -1,6 +1,8 @@
 """Kernel shapes, launch tuning and CUDA-graph capture (needs a GB300).
 
-Every compiled kernel shape, every CTA-per-SM count and every tile side must
+Every compiled kernel shape and build (a request for more CTAs per SM than the
+plain build fits runs the register-capped build of the shapes that have one),
+every CTA-per-SM count and every tile side must
 give results identical to the oracle's; a captured graph must give the same
 results as the direct call, also after its input buffers are refilled with a
 different batch.
@@ -57,7 +59,7 @@ def test_every_kernel_shape_bit_exact(ctx, b):
     base = ctx.tuning
     try:
         for shape in SHAPES[b]:
-            for ctas in (0, 1):
+            for ctas in (0, 1, 64):  # 64: as many as any build fits
                 ctx.tuning = _with_shape(base, b, shape, ctas)
                 got = ctx.tuning
                 assert (got["threads"][b], got["slots_per_thread"][b]) == shape
