@@ -41,24 +41,27 @@ ALGO, RADIUS = -1, 0.4
 WORKLOADS = {
     "mixed": dict(
         events=4096, make=lambda n: E.mixed_batch(n, 50, 2000, seed=3), flush=True, cpu_start=64,
-        per_event_sample=256, second=None,
+        per_event_sample=256, second=None, dominant=(1024, 2048, "k_cluster_smem, events of 1025-2048 particles"),
         metric="events/s, batched anti-kt R=0.4 clustering of 4096 events (50-2000 particles)",
         workload="4096 events, particle counts log-uniform in [50, 2000], anti-kt R=0.4, FP64, one batched call"),
     "pileup": dict(
         events=64, make=lambda n: E.pileup_batch(n, 10000, 60000, seed=4), flush=False, cpu_start=16,
-        per_event_sample=4, second=(1, 0.6),
+        per_event_sample=4, second=(1, 0.6), dominant=None,
         metric="events/s, batched anti-kt R=0.4 clustering of 64 pile-up events (10k-60k particles)",
         workload="64 pile-up-like events, 10k-60k particles, anti-kt R=0.4 (kt R=0.6 beside it), FP64, "
                  "one batched call"),
 }
 WORKLOADS["serving"] = dict(
     events=3000, make=lambda n: E.serving_mix(n, seed=5)[0], flush=False, cpu_start=32, per_event_sample=64,
-    second=None,
+    second=None, dominant=None,
     metric="events/s served, open-loop Poisson arrivals of single events (lognormal sizes, median 1500), "
            "with p50/p99 latency",
     workload="served requests: sizes lognormal (median 1500, sigma 0.8) clipped to [100, 20000]; anti-kt R=0.4 "
              "70%, kt R=0.6 15%, C/A R=0.8 15%; Poisson arrivals at 20k-200k events/s")
 SERVING_RATES = (20000, 50000, 100000, 200000)
+# DRAM bytes per particle of a shared-memory clustering launch (read + write),
+# from the ncu capture summarised in profiles/cluster_smem_mixed_full.md
+TRAFFIC_B_PER_PARTICLE = 33.0
 W = WORKLOADS["mixed"]
 N_EVENTS = W["events"]
 METRIC = W["metric"]
@@ -125,6 +128,46 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def fp64_peak_tflops(dev):
+    """FP64 peak measured here: cuBLAS DGEMM 4096^3 (2 n^3 flops), best of 5, CUDA events."""
+    import torch
+    n = 4096
+    g = torch.Generator(device=dev).manual_seed(0)
+    a = torch.rand((n, n), dtype=torch.float64, device=dev, generator=g)
+    b = torch.rand((n, n), dtype=torch.float64, device=dev, generator=g)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_.record()
+        torch.matmul(a, b)
+        e_.record()
+        e_.synchronize()
+        best = min(best, s_.elapsed_time(e_))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def pair_evaluations(batch, cores, sample=None):
+    """Algorithmic pair evaluations E_pairs of the batch, counted by the CPU
+    nearest-neighbour oracle on the same inputs: N(N-1)/2 initial distances,
+    then per step the new jet against the n_s active pseudojets and one scan of
+    n_s for every pseudojet whose neighbour was merged.  With `sample`, only the
+    `sample` smallest events are counted and the count is scaled by sum N^2."""
+    import oracle
+    sizes = batch.sizes().astype(np.float64)
+    if sample is None or sample >= batch.n_events:
+        return float(oracle.cluster_batch(batch.particles, batch.offsets, ALGO, RADIUS, threads=cores,
+                                          want_history=False)[-1]), "counted"
+    idx = np.argsort(sizes)[:sample]
+    sub = E._batch_from([batch.event(int(e)) for e in idx])
+    ev = oracle.cluster_batch(sub.particles, sub.offsets, ALGO, RADIUS, threads=cores, want_history=False)[-1]
+    return float(ev) * float((sizes ** 2).sum() / (sizes[idx] ** 2).sum()), \
+        f"counted on the {sample} smallest events, scaled by sum N^2"
 
 
 def cpu_cluster_rate(batch, threads, target_s=10.0, max_events=None, algo=None, radius=None):
@@ -221,9 +264,11 @@ def run_ours(args, rank, world, local_rank):
             for k in range(k_steps):
                 if W["flush"]:
                     flush.fill_(float(k))  # evict L2 between steps (inputs are ~70 MB < 129 MB L2)
+                torch.cuda.nvtx.range_push("timed_step")
                 starts[k].record(stream)
                 step(algo, radius)
                 ends[k].record(stream)
+                torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         return [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
 
@@ -251,13 +296,16 @@ def run_ours(args, rank, world, local_rank):
     # end to end through the host-memory entry point (pinned buffers)
     p4_h = torch.from_numpy(batch.particles).pin_memory().numpy()
     off_h = torch.from_numpy(batch.offsets).pin_memory().numpy()
+    out_h = {"jets": torch.empty((total, 4), dtype=torch.float64).pin_memory().numpy(),
+             "jet_label": torch.empty(total, dtype=torch.int32).pin_memory().numpy(),
+             "n_jets": torch.empty(N_EVENTS, dtype=torch.int32).pin_memory().numpy()}
     for _ in range(2):
-        ctx.cluster_batch(p4_h, off_h, ALGO, RADIUS)
+        ctx.cluster_batch(p4_h, off_h, ALGO, RADIUS, out=out_h)
     barrier()
     t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 5))
     for _ in range(e2e_steps):
-        res = ctx.cluster_batch(p4_h, off_h, ALGO, RADIUS)
+        res = ctx.cluster_batch(p4_h, off_h, ALGO, RADIUS, out=out_h)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     if world > 1:
         import torch.distributed as dist
@@ -296,16 +344,58 @@ def run_ours(args, rank, world, local_rank):
                   "ms_per_step": float(np.mean(ms2))}
     d2h = total * 32 + total * 4 + N_EVENTS * 4
 
-    # roofline of the clustering kernels: algorithmic HBM bytes per step
+    # roofline.  Primary: algorithmic FP64 work of the dominant kernel (9 flops
+    # per pair evaluation, pair evaluations counted by the CPU oracle on the
+    # same events) per launch / its launch time, against the FP64 peak measured
+    # here with DGEMM.  Secondary: shared-memory bytes of the same work (24 B
+    # per pair evaluation: rap, phi, w of the partner) against the nominal
+    # shared-memory bandwidth, and the HBM staging bytes of the whole step.
     alg_bytes = 32 * total + 8 * (N_EVENTS + 1) + 36 * n_jets_total + 4 * N_EVENTS
     step_s = dev_s / args.steps
     peak, peak_kind = _peaks()
     achieved = alg_bytes / step_s / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get("bytes_per_step")
+    cores = os.cpu_count() or 1
+    dom = W.get("dominant")
+    if dom is not None:
+        lo_n, hi_n, dom_name = dom
+        sizes_all = batch.sizes()
+        sel = np.flatnonzero((sizes_all > lo_n) & (sizes_all <= hi_n))
+        dom_batch = E._batch_from([batch.event(int(e)) for e in sel])
+        p4_d = torch.from_numpy(dom_batch.particles).to(dev)
+        off_d = torch.from_numpy(dom_batch.offsets).to(dev)
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                ctx.cluster_batch_device(p4_d, off_d, ALGO, RADIUS)
+        ctx.check()
+        dms = []
+        with torch.cuda.stream(stream):
+            for k in range(3):
+                flush.fill_(float(k))
+                s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.nvtx.range_push("dominant_kernel")  # profilers can select these launches
+                s_.record(stream)
+                ctx.cluster_batch_device(p4_d, off_d, ALGO, RADIUS)
+                e_.record(stream)
+                torch.cuda.nvtx.range_pop()
+                e_.synchronize()
+                dms.append(s_.elapsed_time(e_))
+        ctx.check()
+        dom_s = float(np.mean(dms)) / 1e3
+        e_pairs, e_how = pair_evaluations(dom_batch, cores)
+        dom_desc = f"{dom_name} ({dom_batch.n_events} events, {int(dom_batch.offsets[-1])} particles), " \
+                   f"timed alone on its events (CUDA events, 3 launches)"
+        dom_particles = int(dom_batch.offsets[-1])
+    else:
+        dom_s = step_s
+        e_pairs, e_how = pair_evaluations(batch, cores, sample=4 if N_EVENTS > 512 or total > 10 ** 6 else None)
+        dom_desc = "k_cluster_tiled (every event of the batch: one launch per step)"
+        dom_particles = total
+    fp64_peak = fp64_peak_tflops(dev)
+    fp64_ach = 9.0 * e_pairs / dom_s / 1e12
+    smem_peak = 128.0 * 152 * 2.07e9 / 1e12  # TB/s, nominal: 128 B per clock per SM at 2070 MHz
+    # DRAM bytes per particle of the shared-memory kernels from the committed
+    # ncu capture (profiles/cluster_smem_mixed_full.md), scaled to this launch
+    traffic = TRAFFIC_B_PER_PARTICLE * dom_particles if dom is not None else None
     line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * step_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -317,17 +407,26 @@ def run_ours(args, rank, world, local_rank):
             "per_event_launch": per_event,
             "e2e": {"value": world * N_EVENTS / e2e_s, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "note": f"peak {peak_kind}; the kernels are latency-bound (sequential merge steps), "
-                                 f"HBM carries only staging ({alg_bytes} B per step)"},
+            "roofline": {"bound": "fp64", "kernel": dom_desc, "achieved": fp64_ach, "peak": fp64_peak,
+                         "unit": "TFLOP/s", "frac": fp64_ach / fp64_peak, "traffic": traffic,
+                         "pair_evaluations": e_pairs, "pair_evaluations_how": e_how,
+                         "launch_ms": 1e3 * dom_s,
+                         "note": "achieved = 9 flops x E_pairs (oracle count) / launch time; peak measured here "
+                                 "(cuBLAS DGEMM 4096^3); the kernels take most pair decisions in FP32 with a "
+                                 "proven error bound, so this is algorithmic FP64 work, not FP64 instructions",
+                         "secondary": [
+                             {"bound": "smem", "achieved": 24.0 * e_pairs / dom_s / 1e12, "peak": smem_peak,
+                              "unit": "TB/s", "frac": 24.0 * e_pairs / dom_s / 1e12 / smem_peak,
+                              "note": "24 B per pair evaluation; peak nominal (128 B/clk/SM, 152 SMs, 2070 MHz)"},
+                             {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                              "frac": achieved / peak,
+                              "note": f"whole step, staging only ({alg_bytes} B per step); peak {peak_kind}"}]},
             "gpu_launches": args.steps * 9,  # 4 bucketing kernels, the tiled kernel, 4 bucket kernels
             "clocks": clk.summary(),
             "wall_s": t_wall}
     if second is not None:
         line["config"]["second"] = second
     if rank == 0 and not args.no_cpu_baseline:
-        cores = os.cpu_count() or 1
         v, n, dt = cpu_cluster_rate(batch, cores, target_s=10.0)
         line["cpu_baseline"] = {"value": v, "unit": "events/s", "cores": cores, "kind": "port",
                                 "sample": f"first {n} of the {N_EVENTS} events ({dt:.1f} s), oracle "

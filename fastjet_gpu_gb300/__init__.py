@@ -207,13 +207,16 @@ class Context:
         torch.cuda.ExternalStream(self.stream, device=device).wait_stream(torch.cuda.current_stream(device))
 
     # ------------------------------------------------------------ host memory
-    def cluster_batch(self, particles, offsets, algo, radius, history=False, owner=False):
+    def cluster_batch(self, particles, offsets, algo, radius, history=False, owner=False, out=None):
         """Cluster a CSR batch held in host memory; returns numpy arrays.
 
         particles float64 [total, 4]; offsets int64 [n_events + 1]; algo and
         radius are scalars or per-event arrays.  Returns a dict with ``jets``
         [total, 4], ``jet_label`` [total], ``n_jets`` [n_events] and, when
-        requested, ``history`` (STEP records) and ``owner``.
+        requested, ``history`` (STEP records) and ``owner``.  ``out`` may pass
+        preallocated output arrays under those keys (C-contiguous, of those
+        dtypes and at least those lengths; page-locked memory makes the copies
+        back direct), which are filled and returned as views.
         """
         p4 = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 4)
         off = np.ascontiguousarray(offsets, dtype=np.int64)
@@ -221,12 +224,22 @@ class Context:
         total = int(off[-1]) if ne >= 0 else 0
         a_arr = None if np.isscalar(algo) else np.ascontiguousarray(algo, dtype=np.int32)
         r_arr = None if np.isscalar(radius) else np.ascontiguousarray(radius, dtype=np.float64)
-        res = {"jets": np.zeros((max(total, 1), 4)), "jet_label": np.zeros(max(total, 1), np.int32),
-               "n_jets": np.zeros(max(ne, 1), np.int32)}
+        want = {"jets": ((max(total, 1), 4), np.float64), "jet_label": ((max(total, 1),), np.int32),
+                "n_jets": ((max(ne, 1),), np.int32)}
         if history:
-            res["history"] = np.zeros(max(total, 1), STEP)
+            want["history"] = ((max(total, 1),), STEP)
         if owner:
-            res["owner"] = np.zeros(max(total, 1), np.int32)
+            want["owner"] = ((max(total, 1),), np.int32)
+        res = {}
+        for k, (shape, dt) in want.items():
+            a = None if out is None else out.get(k)
+            if a is None:
+                res[k] = np.zeros(shape, dt)
+                continue
+            if (not isinstance(a, np.ndarray) or a.dtype != np.dtype(dt) or not a.flags.c_contiguous
+                    or a.shape[1:] != shape[1:] or a.shape[0] < shape[0]):
+                raise ValueError(f"out[{k!r}] must be a C-contiguous {np.dtype(dt)} array of shape {shape} or longer")
+            res[k] = a
         out = _Outputs(_np_ptr(res["jets"]).value, _np_ptr(res["jet_label"]).value, _np_ptr(res["n_jets"]).value,
                        _np_ptr(res["history"]).value if history else None,
                        _np_ptr(res["owner"]).value if owner else None)

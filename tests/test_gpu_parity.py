@@ -175,3 +175,27 @@ def test_too_big_is_reported(ctx):
     assert st == 4
     ev = E.single_event(100, 2, seed=1)
     ctx.cluster_batch(ev, np.array([0, 100]), -1, 0.4)  # the context stays usable
+
+
+def test_host_entry_preallocated_outputs(ctx):
+    """cluster_batch(out=...) fills the caller's (page-locked) arrays with the
+    same results, and rejects arrays of the wrong dtype or length."""
+    import torch
+    b = E.mixed_batch(30, 50, 1500, seed=51)
+    ref = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, history=True)
+    total = int(b.offsets[-1])
+    out = {"jets": torch.empty((total, 4), dtype=torch.float64).pin_memory().numpy(),
+           "jet_label": torch.empty(total, dtype=torch.int32).pin_memory().numpy(),
+           "n_jets": torch.empty(b.n_events, dtype=torch.int32).pin_memory().numpy()}
+    got = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, history=True, out=out)
+    assert np.array_equal(got["n_jets"], ref["n_jets"])
+    assert np.array_equal(got["history"], ref["history"])
+    for e in range(b.n_events):  # rows past an event's jet count are not written
+        o, nj = b.offsets[e], ref["n_jets"][e]
+        assert np.array_equal(got["jets"][o:o + nj], ref["jets"][o:o + nj]), e
+        assert np.array_equal(got["jet_label"][o:o + nj], ref["jet_label"][o:o + nj]), e
+    assert got["jets"].ctypes.data == out["jets"].ctypes.data
+    with pytest.raises(ValueError):
+        ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, out={"jets": np.zeros((total, 4), np.float32)})
+    with pytest.raises(ValueError):
+        ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, out={"n_jets": np.zeros(b.n_events - 1, np.int32)})
