@@ -61,7 +61,7 @@ WORKLOADS["serving"] = dict(
 SERVING_RATES = (20000, 50000, 100000, 200000)
 # DRAM bytes per particle of a shared-memory clustering launch (read + write),
 # from the ncu capture summarised in profiles/cluster_smem_mixed_full.md
-TRAFFIC_B_PER_PARTICLE = 33.0
+TRAFFIC_B_PER_PARTICLE = 58.7
 W = WORKLOADS["mixed"]
 N_EVENTS = W["events"]
 METRIC = W["metric"]

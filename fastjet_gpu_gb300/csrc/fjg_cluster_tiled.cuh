@@ -63,7 +63,8 @@ constexpr int kListSlack = 64;      // spare list entries per possible tile
 constexpr int kTileSlackMax = 256;  // rebuild interval bound (steps)
 constexpr int kMaxTiles = 4096;
 constexpr int kMaxWindowTiles = 9;
-constexpr int kMaxListed = 4 * kMaxTargets;  // targets recorded in S2
+constexpr int kTiledTargets = 32;                // targets per step scanned during the merge
+constexpr int kMaxListed = 4 * kTiledTargets;  // targets recorded in S2
 constexpr int kMaxDirty = 64;
 constexpr int kLargeWsBytesPerParticle = 96;  // bound of large_ws_bytes(N) / N for N > 2048
 
@@ -193,7 +194,7 @@ struct TiledShared {
   Cand wcand[W];
   Arg wexact[W];
   Cert wcert[W];
-  Cert rcert[kMaxTargets][W];
+  Cert rcert[kTiledTargets][W];
   int rlist[kMaxListed];
   int n_rescan;
   int dirty[kMaxDirty];
@@ -844,7 +845,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
         }
       }
       named_sync(1, TR);
-      const int nr = min(S.n_rescan, kMaxTargets);
+      const int nr = min(S.n_rescan, kTiledTargets);
       for (int r = 0; r < nr; ++r) {
         Cert rc = cert_empty();
         window_cert(S, L, X, S.rlist[r], r0, TR, c, j, rc);
@@ -858,7 +859,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     if (n == 0) break;
     const int n_found = S.n_rescan;
     const int nr_all = min(n_found, kMaxListed);
-    const int nr = min(nr_all, kMaxTargets);
+    const int nr = min(nr_all, kTiledTargets);
     const int ta = pair ? S.ta_u * S.nphi + S.ta_v : -1;
 
     // S3a: tile lists (thread 0: a tombstone for b, and for a when it
