@@ -134,8 +134,30 @@ def lib():
         L.fjg_server_release.argtypes = [P, ctypes.c_uint64]
         L.fjg_server_pending.argtypes = [P]
         L.fjg_server_replay.argtypes = [P, P, P, I, P, P, P, P, ctypes.POINTER(D)]
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        L.fjg_parse_events.argtypes = [P, ctypes.c_size_t, I, P, ctypes.c_int64, P, ctypes.c_int64, i64p, i64p, i64p]
         _lib = L
     return _lib
+
+
+def parse_events(text, threads=0):
+    """Read the reference driver's event text (bytes or str) into CSR arrays
+    with the native multi-threaded reader (fjg_parse_events: same rules and
+    values as events.read_events).  Returns (particles float64 [total, 4],
+    offsets int64 [n_events + 1]); ValueError names the rejected line.  Host
+    only: no GPU needed."""
+    buf = text.encode() if isinstance(text, str) else bytes(text)
+    cap = buf.count(b"\n") + 1  # particles <= lines, events + 1 <= lines + 1
+    parts = np.empty((cap, 4), np.float64)
+    offs = np.empty(cap + 1, np.int64)
+    npart, nev, bad = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+    st = lib().fjg_parse_events(buf, len(buf), int(threads), _np_ptr(parts), cap, _np_ptr(offs), cap + 1,
+                                ctypes.byref(npart), ctypes.byref(nev), ctypes.byref(bad))
+    if st == 1 and bad.value > 0:
+        raise ValueError(lib().fjg_last_error(None).decode())
+    if st:
+        raise FjgError(st, lib().fjg_last_error(None).decode())
+    return parts[:npart.value].copy(), offs[:nev.value + 1].copy()
 
 
 def _np_ptr(a):

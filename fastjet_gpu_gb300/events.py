@@ -143,10 +143,12 @@ def serving_mix(n_events, seed=5, median=1500.0, sigma=0.8, lo=100, hi=20000):
 def read_events(path_or_text):
     """Parse the reference driver's event stream into a list of [n, 4] arrays.
 
-    Follows main.cc:34-70: leading '#' and blank lines are skipped, each line
-    holds px py pz E, an event ends at the first line that does not parse as
-    four numbers; such a line must be blank or start with '#', otherwise a
-    ValueError is raised (main.cc:55-58 throws).
+    Follows main.cc:34-70: each line holds px py pz E (anything after the
+    fourth number is ignored); an event is a maximal run of such lines; an
+    empty line or one starting with '#' ends an event; any other line raises
+    ValueError (main.cc:55-58 throws); a final line without a newline is not
+    read (the reference's getline loop stops at end of file).  Numbers take an
+    optional sign and no inf/nan, as istream >> double reads them.
     """
     if "\n" in path_or_text or not path_or_text:
         text = path_or_text
@@ -154,27 +156,39 @@ def read_events(path_or_text):
         with open(path_or_text) as f:
             text = f.read()
     events, cur = [], []
-    for line in text.split("\n"):
-        fields = line.split()
-        vals = None
-        if len(fields) >= 4:
-            try:
-                vals = [float(x) for x in fields[:4]]
-            except ValueError:
-                vals = None
-        if vals is not None:
-            cur.append(vals)
+    lines = text.split("\n")[:-1]  # the piece after the last newline is not read
+    for line in lines:
+        if not line or line[0] == "#":
+            if cur:
+                events.append(np.array(cur, dtype=np.float64))
+                cur = []
             continue
-        if line and line[0] != "#" and cur:
+        vals = _particle_line(line)
+        if vals is None:
             raise ValueError("Error while parsing particles:\n" + line)
-        if line and line[0] != "#" and not cur and line.strip():
-            raise ValueError("Error while parsing particles:\n" + line)
-        if cur:
-            events.append(np.array(cur, dtype=np.float64))
-            cur = []
+        cur.append(vals)
     if cur:
         events.append(np.array(cur, dtype=np.float64))
     return events
+
+
+_NUMBER = None
+
+
+def _particle_line(line):
+    """The first four numbers of a line as istream >> double reads them, or None."""
+    global _NUMBER
+    if _NUMBER is None:
+        import re
+        _NUMBER = re.compile(r"[ \t\r\v\f]*([+-]?(?:[0-9]+\.?[0-9]*|\.[0-9]+)(?:[eE][+-]?[0-9]+)?)")
+    vals, pos = [], 0
+    for _ in range(4):
+        m = _NUMBER.match(line, pos)
+        if not m:
+            return None
+        vals.append(float(m.group(1)))
+        pos = m.end()
+    return vals
 
 
 def write_events(events, path=None):

@@ -208,6 +208,25 @@ fjg_status fjg_set_tuning(fjg_ctx* ctx, const fjg_tuning* tuning);
 #define FJG_TUNE_SKIP_LARGE 1
 fjg_status fjg_autotune(fjg_ctx* ctx, int algo, double r, int flags, fjg_tuning* result);
 
+/* ------------------------------------------------------------ event text
+ * Reads the reference driver's input format (main.cc:34-70) into CSR arrays:
+ * one particle per line, "px py pz E" (whitespace separated; anything after
+ * the fourth number is ignored); an event is a maximal run of such lines; an
+ * empty line or one starting with '#' ends an event; any other line is
+ * rejected, as the reference's reader throws on it; a final line without a
+ * newline is not read (the reference's getline loop stops there).  Numbers are correctly
+ * rounded decimals with an optional sign (no inf/nan), the values
+ * istream >> double gives.  `particles` receives [n_particles][4] doubles,
+ * `offsets` n_events + 1 entries (offsets[0] = 0).  Host only: no context or
+ * device is involved; `threads` <= 0 uses every hardware thread (texts below
+ * 1 MiB are read by one).  FJG_EINVAL with *error_line (1-based) on a rejected
+ * line; FJG_ETOOBIG when max_particles or max_offsets is too small, with
+ * *n_particles and *n_events set to what is needed.  Replaces the driver's
+ * read_n_events (main.cc:76-85) for callers of the library. */
+fjg_status fjg_parse_events(const char* text, size_t len, int threads, double* particles, int64_t max_particles,
+                            int64_t* offsets, int64_t max_offsets, int64_t* n_particles, int64_t* n_events,
+                            int64_t* error_line);
+
 /* ------------------------------------------------------------ serving
  * No counterpart in the reference.  A request server on one context: events
  * are submitted one at a time as they arrive and complete independently.
