@@ -140,6 +140,7 @@ __device__ __forceinline__ Cand cand_warp(const Cand& c) {
 struct LargeWs {
   float *rap32, *phi32, *wlo, *whi, *nlo, *nhi, *klo, *khi;  // [N]
   int *nn, *tile, *pos;                                       // [N]
+  int* rc;                                                    // [N] slots whose neighbour this is
   int8_t *pair, *alive;                                       // [N]
   int* members;                                               // [N + kListSlack * MT]
   int *t_start, *t_count;                                     // [MT]
@@ -152,7 +153,7 @@ __host__ __device__ __forceinline__ int large_max_tiles(int N) { return (N / 8 <
 
 __host__ __device__ __forceinline__ int64_t large_ws_bytes(int N) {
   const int64_t MT = large_max_tiles(N);
-  const int64_t head = 8 * 4 * (int64_t)N + 3 * 4 * (int64_t)N + ((2 * (int64_t)N + 15) & ~(int64_t)15);
+  const int64_t head = 8 * 4 * (int64_t)N + 4 * 4 * (int64_t)N + ((2 * (int64_t)N + 15) & ~(int64_t)15);
   return head + 4 * ((int64_t)N + kListSlack * MT) + 2 * 4 * MT + 16 + 32 * MT;
 }
 
@@ -172,7 +173,8 @@ __device__ __forceinline__ LargeWs large_ws(unsigned char* base, int N) {
   L.nn = i;
   L.tile = i + N;
   L.pos = i + 2 * N;
-  int8_t* b = reinterpret_cast<int8_t*>(i + 3 * N);
+  L.rc = i + 3 * N;
+  int8_t* b = reinterpret_cast<int8_t*>(i + 4 * N);
   L.pair = b;
   L.alive = b + N;
   int* m = reinterpret_cast<int*>(b + ((2 * N + 15) & ~15));
@@ -190,6 +192,7 @@ struct TiledShared {
   static constexpr int W = kTiledT / 32;
   double rmin, inv_side_r, inv_side_phi;
   int nrap, nphi, nt, slack;
+  int rc_a_old, rc_drop;  // referrer-count updates of the step
   int ta_u, ta_v;  // tile of the new jet (rapidity and azimuth index)
   Cand wcand[W];
   Arg wexact[W];
@@ -545,6 +548,7 @@ __device__ __forceinline__ void rescan_warp(TiledShared& S, const LargeWs& L, co
   float lo, hi;
   const int nn = resolve_large(S, L, X, t, x, skip, -1, -1, lo, hi);
   if (lane == 0) {
+    if (nn >= 0) atomicAdd(&L.rc[nn], 1);  // t's old neighbour was a merged slot
     L.nn[t] = nn;
     L.nlo[t] = lo;
     L.nhi[t] = hi;
@@ -654,6 +658,8 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   rebuild_tiles(S, L, N, false);
 
   // ---- initial nearest neighbours within the windows
+  for (int s = tid; s < N; s += T) L.rc[s] = 0;
+  __syncthreads();
   for (int t = tid; t < N; t += T) {
     Cert c = cert_empty();
     window_cert(S, L, X, t, 0, 1, -1, -1, c);
@@ -690,6 +696,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     L.nn[t] = nn;
     L.nlo[t] = nlo;
     L.nhi[t] = nhi;
+    if (nn >= 0) atomicAdd(&L.rc[nn], 1);
   }
   __syncthreads();
   for (int t = tid; t < N; t += T) set_key_large(L, X, t);
@@ -823,34 +830,48 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       __syncwarp();
     } else {
       // targets: live slots other than c, j whose neighbour is c or j; they
-      // lie in the windows of c's and j's tiles
+      // lie in the windows of c's and j's tiles.  The referrer counts say how
+      // many there are (c's neighbour is j for a pair, and j's may be c):
+      // without any, the scan is skipped (the same values for every thread)
       const int r0 = tid - 32 * MW;
-      int tiles[2 * kMaxWindowTiles];
-      const int nw = window_union(S, tile_c, tile_j, tiles);
-      constexpr int NU = 2 * kMaxWindowTiles;
-      const TileRanges<NU> R = tile_ranges<NU>(L, tiles, nw);
-      for (int i = r0; i < R.maxlen; i += TR) {
-        int u[NU], nu[NU];
-#pragma unroll
-        for (int k = 0; k < NU; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
-#pragma unroll
-        for (int k = 0; k < NU; ++k) nu[k] = u[k] >= 0 ? L.nn[u[k]] : -1;
-#pragma unroll
-        for (int k = 0; k < NU; ++k) {
-          if (u[k] < 0 || u[k] == c || u[k] == j) continue;
-          if (nu[k] == c || (pair && nu[k] == j)) {
-            const int p = atomicAdd(&S.n_rescan, 1);
-            if (p < kMaxListed) S.rlist[p] = u[k];
+      const int rcc = L.rc[c], rcj = pair ? L.rc[j] : 0, nnj = pair ? L.nn[j] : -1;
+      const int expected = pair ? rcc + rcj - 1 - (nnj == c ? 1 : 0) : rcc;
+      if (r0 == 0) {
+        // referrer counts this step retires (applied after B2, read before
+        // any update): the new jet's slot loses its old referrers (the
+        // targets, which count again under their new neighbours), and the
+        // merged slots' own old neighbours lose one each
+        S.rc_a_old = pair ? (a == c ? rcc : rcj) : 0;
+        S.rc_drop = pair ? ((nnj != c && nnj != j) ? nnj : -1) : L.nn[c];
+      }
+      if (expected > 0) {
+        int tiles[2 * kMaxWindowTiles];
+        const int nw = window_union(S, tile_c, tile_j, tiles);
+        constexpr int NU = 2 * kMaxWindowTiles;
+        const TileRanges<NU> R = tile_ranges<NU>(L, tiles, nw);
+        for (int i = r0; i < R.maxlen; i += TR) {
+          int u[NU], nu[NU];
+  #pragma unroll
+          for (int k = 0; k < NU; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
+  #pragma unroll
+          for (int k = 0; k < NU; ++k) nu[k] = u[k] >= 0 ? L.nn[u[k]] : -1;
+  #pragma unroll
+          for (int k = 0; k < NU; ++k) {
+            if (u[k] < 0 || u[k] == c || u[k] == j) continue;
+            if (nu[k] == c || (pair && nu[k] == j)) {
+              const int p = atomicAdd(&S.n_rescan, 1);
+              if (p < kMaxListed) S.rlist[p] = u[k];
+            }
           }
         }
-      }
-      named_sync(1, TR);
-      const int nr = min(S.n_rescan, kTiledTargets);
-      for (int r = 0; r < nr; ++r) {
-        Cert rc = cert_empty();
-        window_cert(S, L, X, S.rlist[r], r0, TR, c, j, rc);
-        const Cert wc = cert_warp(rc);
-        if (lane == 0) S.rcert[r][warp] = wc;
+        named_sync(1, TR);
+        const int nr = min(S.n_rescan, kTiledTargets);
+        for (int r = 0; r < nr; ++r) {
+          Cert rc = cert_empty();
+          window_cert(S, L, X, S.rlist[r], r0, TR, c, j, rc);
+          const Cert wc = cert_warp(rc);
+          if (lane == 0) S.rcert[r][warp] = wc;
+        }
       }
     }
     __syncthreads();  // B2
@@ -865,6 +886,8 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     // S3a: tile lists (thread 0: a tombstone for b, and for a when it
     // changes tile, then an append); targets (one warp each)
     if (tid == 0) {
+      if (pair) atomicSub(&L.rc[a], S.rc_a_old);
+      if (S.rc_drop >= 0) atomicSub(&L.rc[S.rc_drop], 1);
       L.members[L.t_start[L.tile[b]] + L.pos[b]] = -1;
       L.alive[b] = 0;
       mark_dirty(S, L.tile[b]);
@@ -899,6 +922,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       float lo, hi;
       const int nn = resolve_large(S, L, X, t, x, c, j, extra, lo, hi);
       if (lane == 0) {
+        if (nn >= 0) atomicAdd(&L.rc[nn], 1);
         L.nn[t] = nn;
         L.nlo[t] = lo;
         L.nhi[t] = hi;
@@ -924,7 +948,12 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           while (ball) {
             const int src = __ffs(ball) - 1;
             ball &= ball - 1;
-            rescan_warp(S, L, X, __shfl_sync(kFull, u, src), b);
+            const int t = __shfl_sync(kFull, u, src);
+            // a listed target whose new neighbour is the new jet in a merged
+            // slot is found again: it is done (and counted) already
+            bool listed = false;
+            for (int q = lane; q < kMaxListed; q += 32) listed |= S.rlist[q] == t;
+            if (!__any_sync(kFull, listed)) rescan_warp(S, L, X, t, b);
           }
         }
       }
@@ -977,6 +1006,8 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
             uhi = fjk_to_f32(da, 2);
           }
           if (closer) {
+            if (cn[k] >= 0) atomicSub(&L.rc[cn[k]], 1);
+            atomicAdd(&L.rc[a], 1);
             L.nn[t] = a;
             L.nlo[t] = ulo;
             L.nhi[t] = uhi;
@@ -998,6 +1029,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       float lo, hi;
       const int nn = resolve_large(S, L, X, a, x, b, -1, -1, lo, hi);
       if (lane == 0) {
+        if (nn >= 0) atomicAdd(&L.rc[nn], 1);
         L.nn[a] = nn;
         L.nlo[a] = lo;
         L.nhi[a] = hi;
