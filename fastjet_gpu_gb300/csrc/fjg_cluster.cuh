@@ -72,6 +72,7 @@ struct BatchArgs {
   int* status;             // device error flag (0 = ok)
   unsigned char* large_ws; // tiled-path workspace: event e at large_ws + 96 * offsets[e] (null: none)
   double tile_factor;      // tiled path: tile side >= tile_factor * R (>= 1)
+  int serve_order;         // launch priority (host side): 0 largest events first, 1 smallest first
   int pairs;               // offsets hold (start, end) pairs: events need not be contiguous
   int* done;               // null, or completion flags: done[done_slot[e]] = 1 (system scope) per event
   const int32_t* done_slot;

@@ -62,6 +62,7 @@ constexpr int kTiledT = 256;
 constexpr int kListSlack = 64;      // spare list entries per possible tile
 constexpr int kTileSlackMax = 256;  // rebuild interval bound (steps)
 constexpr int kMaxTiles = 4096;
+constexpr double kTileMembers = 32.0;  // particles per tile the tile side aims at (at least)
 constexpr int kMaxWindowTiles = 9;
 constexpr int kTiledTargets = 32;                // targets per step scanned during the merge
 constexpr int kMaxListed = 4 * kTiledTargets;  // targets recorded in S2
@@ -623,7 +624,12 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     lo = fmax(lo, -15.0);
     hi = fmin(hi, 15.0);
     if (!(hi >= lo)) hi = lo;
-    const double side_min = R * fmax(A.tile_factor, 1.0) * (1.0 + 1e-4) + 1e-5;
+    // tile side: at least R (times the tuning factor), and large enough that
+    // a tile holds about kTileMembers particles on average, so that sparse
+    // events do not scan mostly empty windows
+    const double side_r = R * fmax(A.tile_factor, 1.0) * (1.0 + 1e-4) + 1e-5;
+    const double area = fmax(hi - lo, side_r) * 6.283185307179586;
+    const double side_min = fmax(side_r, sqrt(area * kTileMembers / (double)N));
     int nphi = (int)fmin(floor(6.283185307179586 / side_min), 4096.0);
     nphi = nphi < 1 ? 1 : nphi;
     int nrap = (int)fmin(floor((hi - lo) / side_min), 4096.0);

@@ -40,7 +40,7 @@ int launch_priority(int level) {
 }
 
 cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
-  return launch_with_priority(k_cluster_tiled, grid, kTiledT, 0, s, 0, A);
+  return launch_with_priority(k_cluster_tiled, grid, kTiledT, 0, s, tiled_priority_level(A.serve_order), A);
 }
 
 // Events are handed to the bucket kernels largest first (longest-processing-

@@ -71,8 +71,11 @@ bool tuning_valid(const Tuning& t);
 // (level kNumBuckets - b), so that when the bucket kernels of one batch run
 // side by side the SMs take the longest events first and the small buckets
 // fill the tail.  Levels beyond the device's range share its lowest priority.
+// A request server wants the opposite (`serve_order`): its small events are
+// the latency-bound ones, so they go first and the tiled kernel last.
 int launch_priority(int level);
-inline int bucket_priority_level(int b) { return kNumBuckets - b; }
+inline int bucket_priority_level(int b, int serve_order) { return serve_order ? b : kNumBuckets - b; }
+inline int tiled_priority_level(int serve_order) { return serve_order ? kNumBuckets : 0; }
 
 // Launch of a clustering kernel with its priority as a launch attribute
 // (recorded in a captured graph too).

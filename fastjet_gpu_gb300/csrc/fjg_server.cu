@@ -197,6 +197,7 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
   A.status = L.d_status;
   A.large_ws = S->d_large;
   A.tile_factor = ctx->tune.tile_factor;
+  A.serve_order = 1;  // small events first: they are the latency-bound requests
   A.done = S->d_done;
   A.done_slot = L.dev.done_slot;
   cudaError_t err = cudaMemsetAsync(L.d_queue, 0, 2 * sizeof(int), L.stream);  // queue head and status

@@ -81,7 +81,7 @@ cudaError_t launch_smem(const BatchArgs& A, int grid, cudaStream_t s) {
   cudaError_t err = configure_smem(k_cluster_smem<T, SPT>, sizeof(SmemLayout<T, SPT>), smem_configured<T, SPT>());
   if (err != cudaSuccess) return err;
   return launch_with_priority(k_cluster_smem<T, SPT>, grid, T, sizeof(SmemLayout<T, SPT>), s,
-                              bucket_priority_level(bucket_of(T * SPT)), A);
+                              bucket_priority_level(bucket_of(T * SPT), A.serve_order), A);
 }
 
 template <int T, int SPT, int MINB>
@@ -90,7 +90,7 @@ cudaError_t launch_smem_capped(const BatchArgs& A, int grid, cudaStream_t s) {
                                    smem_configured_capped<T, SPT, MINB>());
   if (err != cudaSuccess) return err;
   return launch_with_priority(k_cluster_smem_capped<T, SPT, MINB>, grid, T, sizeof(SmemLayout<T, SPT>), s,
-                              bucket_priority_level(bucket_of(T * SPT)), A);
+                              bucket_priority_level(bucket_of(T * SPT), A.serve_order), A);
 }
 
 template <int T, int SPT>

@@ -201,9 +201,10 @@ fjg_status fjg_get_tuning(fjg_ctx* ctx, fjg_tuning* tuning);
  * shapes of that bucket's capacity or a field is out of range. */
 fjg_status fjg_set_tuning(fjg_ctx* ctx, const fjg_tuning* tuning);
 /* Time every compiled shape and a few CTA-per-SM counts on synthetic events
- * of each bucket's size range (and, unless flags & FJG_TUNE_SKIP_LARGE, a few
- * tile sides on events of 5000-9000 particles) for `algo` and `r`, keep the
- * fastest, and return the choice in *result (may be NULL).  Takes about a
+ * of each bucket's size range for `algo` and `r`, keep the fastest, and
+ * return the choice in *result (may be NULL).  The tiled kernel's tile side
+ * follows each event's particle density (at least R), so tile_factor is set
+ * to 1; FJG_TUNE_SKIP_LARGE is accepted and has no effect.  Takes about a
  * second per bucket; synchronous. */
 #define FJG_TUNE_SKIP_LARGE 1
 fjg_status fjg_autotune(fjg_ctx* ctx, int algo, double r, int flags, fjg_tuning* result);
