@@ -57,8 +57,8 @@ WORKLOADS["serving"] = dict(
     metric="events/s served, open-loop Poisson arrivals of single events (lognormal sizes, median 1500), "
            "with p50/p99 latency",
     workload="served requests: sizes lognormal (median 1500, sigma 0.8) clipped to [100, 20000]; anti-kt R=0.4 "
-             "70%, kt R=0.6 15%, C/A R=0.8 15%; Poisson arrivals at 20k-200k events/s")
-SERVING_RATES = (20000, 50000, 100000, 200000)
+             "70%, kt R=0.6 15%, C/A R=0.8 15%; Poisson arrivals at 2k-200k events/s (20k-200k as specified, 2k and 4k below capacity)")
+SERVING_RATES = (2000, 4000, 20000, 50000, 100000, 200000)  # the first two below capacity
 # DRAM bytes per particle of a shared-memory clustering launch (read + write),
 # from the ncu capture summarised in profiles/cluster_smem_mixed_full.md
 TRAFFIC_B_PER_PARTICLE = 58.7
