@@ -62,6 +62,9 @@ SERVING_RATES = (2000, 4000, 20000, 50000, 100000, 200000)  # the first two belo
 # DRAM bytes per particle of a shared-memory clustering launch (read + write),
 # from the ncu capture summarised in profiles/cluster_smem_mixed_full.md
 TRAFFIC_B_PER_PARTICLE = 58.7
+# the same for the tiled kernel (profiles/cluster_tiled_pileup2_sections.md:
+# 5.0 MB of DRAM traffic for 103,475 particles)
+TRAFFIC_TILED_B_PER_PARTICLE = 48.3
 W = WORKLOADS["mixed"]
 N_EVENTS = W["events"]
 METRIC = W["metric"]
@@ -395,7 +398,7 @@ def run_ours(args, rank, world, local_rank):
     smem_peak = 128.0 * 152 * 2.07e9 / 1e12  # TB/s, nominal: 128 B per clock per SM at 2070 MHz
     # DRAM bytes per particle of the shared-memory kernels from the committed
     # ncu capture (profiles/cluster_smem_mixed_full.md), scaled to this launch
-    traffic = TRAFFIC_B_PER_PARTICLE * dom_particles if dom is not None else None
+    traffic = (TRAFFIC_B_PER_PARTICLE if dom is not None else TRAFFIC_TILED_B_PER_PARTICLE) * dom_particles
     line = {"metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * step_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
