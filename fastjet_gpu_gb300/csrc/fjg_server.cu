@@ -76,6 +76,7 @@ struct Lane {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev = nullptr;
   bool busy = false;
+  int q = -1;  // queue of the micro-batch in flight
   std::vector<Req*> batch;
   Block host{}, dev{};
   int* d_queue = nullptr;   // work-queue head (device)
@@ -212,6 +213,7 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
   if (err == cudaSuccess) err = cudaMemcpyAsync(L.h_status, L.d_status, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
   if (err == cudaSuccess) err = cudaEventRecord(L.ev, L.stream);
   L.busy = true;
+  L.q = q;
   S->inflight[q] += m;
   return err;
 }
@@ -264,16 +266,20 @@ bool progress(fjg_server* S) {
     r->state = kAdmitted;
     S->admitted[r->bucket].push_back(r);
   }
-  // 3. launches, largest events first
-  for (int q = fjg::kLargeQueue; q >= 0; --q) {
+  // 3. launches, smallest events first (they are the latency-bound
+  // requests); events above 4096 particles take at most half of the streams
+  // and of the SMs (a tiled-kernel CTA fills an SM's registers for the whole
+  // event), so that they cannot hold every SM away from the small ones
+  for (int q = 0; q <= fjg::kLargeQueue; ++q) {
     while (!S->admitted[q].empty() && S->inflight[q] < S->limit[q]) {
       Lane* idle = nullptr;
-      for (Lane& L : S->lanes)
-        if (!L.busy) {
-          idle = &L;
-          break;
-        }
+      int large_lanes = 0;
+      for (Lane& L : S->lanes) {
+        if (L.busy && L.q == fjg::kLargeQueue) ++large_lanes;
+        if (!L.busy && !idle) idle = &L;
+      }
       if (!idle) return true;
+      if (q == fjg::kLargeQueue && 2 * large_lanes >= (int)S->lanes.size()) break;
       const int m = (int)std::min<int64_t>(
           {(int64_t)S->admitted[q].size(), (int64_t)S->cfg.max_batch, (int64_t)(S->limit[q] - S->inflight[q])});
       if (launch_lane(S, *idle, q, m) != cudaSuccess) {
@@ -423,7 +429,7 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
   for (int k = c.max_inflight - 1; k >= 0; --k) S->free_slots.push_back(k);
   for (int q = 0; q < fjg::kNumBuckets; ++q)
     S->limit[q] = c.oversubscribe * ctx->num_sms * std::max(1, fjg::bucket_per_sm(ctx->tune, q));
-  S->limit[fjg::kLargeQueue] = c.oversubscribe * ctx->num_sms * ctx->tune.large_ctas_per_sm;
+  S->limit[fjg::kLargeQueue] = std::max(1, ctx->num_sms / 2);
   *out = S;
   return FJG_OK;
 }

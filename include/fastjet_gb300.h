@@ -242,7 +242,10 @@ fjg_status fjg_parse_events(const char* text, size_t len, int threads, double* p
  *   most `oversubscribe`).
  * - Continuous batching: admitted events of one size bucket are launched
  *   together as a micro-batch on the first idle stream of a pool of
- *   `streams`, while earlier micro-batches are still running; every event
+ *   `streams`, smallest buckets first, while earlier micro-batches are still
+ *   running; events above 4096 particles use at most half of the streams and
+ *   have at most one in flight per two SMs, so that they cannot keep the
+ *   small requests off the GPU; every event
  *   raises its own completion flag in mapped host memory as soon as it is
  *   done, so results do not wait for the rest of their micro-batch.
  * - Progress happens inside fjg_server_submit and fjg_server_poll (no
