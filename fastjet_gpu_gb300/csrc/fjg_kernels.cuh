@@ -9,9 +9,9 @@
 namespace fjg {
 
 // Size buckets of the shared-memory path: bucket b holds events of up to
-// 256 << b particles (45 bytes of shared memory per slot; by default CTAs of
-// 64, 64, 128, 256 and 512 threads with 4, 8, 8, 8 and 8 slots per thread, of
-// which 8, 8, 4, 2 and 1 share an SM).
+// 256 << b particles (36 bytes of shared memory per slot; by default CTAs of
+// 64, 64, 128, 256 and 512 threads with 4, 8, 8, 8 and 8 slots per thread;
+// with the register-capped builds 12, 10, 5, 3 and 1 of them share an SM).
 constexpr int kNumBuckets = 5;
 constexpr int kSmemMaxN = 4096;
 // Events above kSmemMaxN particles form one more work list, run by the tiled
