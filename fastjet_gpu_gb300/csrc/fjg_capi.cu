@@ -38,7 +38,7 @@ fjg_status status_to_error(fjg_ctx* ctx, int st) {
   if (st & kStatusTooBig) return set_error(ctx, FJG_ETOOBIG, "an event exceeds the supported particle count");
   if (st & kStatusInternal)
     return set_error(ctx, FJG_EKERNEL, "a clustering kernel found no candidate (non-finite input?)");
-  return set_error(ctx, FJG_EINVAL, "invalid event offsets");
+  return set_error(ctx, FJG_EINVAL, "an event has a non-finite momentum component, or the event offsets are invalid");
 }
 
 bool valid_algo(int a) { return a == FJG_KT || a == FJG_CAM || a == FJG_ANTIKT; }

@@ -51,9 +51,34 @@ cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
 
 // Events above kSmemMaxN particles go straight to the large list (or raise
 // kStatusTooBig when there is no large workspace, or it is too small).
+// Input check, one warp per event: n_jets[e] = -1 when a momentum component
+// is not finite (the event is then refused: kStatusBadArg), else 0.  Events
+// of no or too many particles are left to the bucketing.
+__global__ void k_check_events(const double* p4, int p4_stride, const int64_t* offsets, int n_events,
+                               int32_t* n_jets) {
+  const int lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int e = w0; e < n_events; e += nw) {
+    const int64_t o0 = offsets[e], o1 = offsets[e + 1];
+    bool bad = false;
+    if (o1 - o0 > 0 && o1 - o0 <= kLargeMaxN) {
+      for (int64_t s = o0 + lane; s < o1; s += 32) {
+        const double* p = p4 + s * p4_stride;
+        bad |= !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) && isfinite(p[3]));
+      }
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) n_jets[e] = bad ? -1 : 0;
+  }
+}
+
 __global__ void k_size_hist(const int64_t* offsets, int n_events, int32_t* hist, int32_t* n_jets, int* status,
                             int32_t* large_order, int32_t* large_count, int64_t large_particles) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
+    if (n_jets[e] < 0) {  // non-finite input (k_check_events); k_size_scatter resets it
+      atomicOr(status, kStatusBadArg);
+      continue;
+    }
     const int64_t n64 = offsets[e + 1] - offsets[e];
     if (n64 > kSmemMaxN) {
       if (n64 <= kLargeMaxN && offsets[e + 1] <= large_particles) {
@@ -153,8 +178,13 @@ __global__ void __launch_bounds__(1024) k_size_scan(int32_t* hist, int32_t* coun
   }
 }
 
-__global__ void k_size_scatter(const int64_t* offsets, int n_events, int32_t* hist, int32_t* order, int cap_events) {
+__global__ void k_size_scatter(const int64_t* offsets, int n_events, int32_t* hist, int32_t* order, int cap_events,
+                               int32_t* n_jets) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
+    if (n_jets[e] < 0) {  // refused: no jets
+      n_jets[e] = 0;
+      continue;
+    }
     const int64_t n64 = offsets[e + 1] - offsets[e];
     if (n64 <= 0 || n64 > kSmemMaxN) continue;
     const int pos = atomicAdd(&hist[n64], 1);
@@ -168,11 +198,13 @@ static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_e
   if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumQueues, stream)) != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(sc.counts + kLargeQueue, 0, sizeof(int32_t), stream)) != cudaSuccess) return err;
   const int grid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
+  const int cgrid = n_events / 8 + 1 > 2048 ? 2048 : n_events / 8 + 1;  // 8 events (warps) per block
+  k_check_events<<<cgrid, 256, 0, stream>>>(base.p4, base.p4_stride, base.offsets, n_events, base.n_jets);
   int32_t* large_order = sc.order + kLargeQueue * sc.cap_events;
   k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status, large_order,
                                         sc.counts + kLargeQueue, sc.large_ws ? sc.large_ws_particles : 0);
   k_size_scan<<<1, 1024, 0, stream>>>(sc.hist, sc.counts);
-  k_size_scatter<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, sc.order, sc.cap_events);
+  k_size_scatter<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, sc.order, sc.cap_events, base.n_jets);
   k_large_sort<<<1, 1024, 0, stream>>>(base.offsets, large_order, sc.counts + kLargeQueue);
   return cudaGetLastError();
 }
@@ -305,6 +337,27 @@ cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int
   return cudaSuccess;
 }
 
+// The single-event path's input check: an event with a non-finite momentum
+// empties every work list (nothing runs) and raises kStatusBadArg.
+__global__ void k_check_single(const double* p4, int p4_stride, int n, int32_t* counts, int32_t* n_jets,
+                               int* status) {
+  __shared__ int any_bad;
+  if (threadIdx.x == 0) any_bad = 0;
+  __syncthreads();
+  bool bad = false;
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    const double* p = p4 + (int64_t)s * p4_stride;
+    bad |= !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) && isfinite(p[3]));
+  }
+  if (bad) any_bad = 1;
+  __syncthreads();
+  if (threadIdx.x == 0 && any_bad) {
+    for (int b = 0; b < kNumQueues; ++b) counts[b] = 0;
+    n_jets[0] = 0;
+    atomicOr(status, kStatusBadArg);
+  }
+}
+
 __global__ void k_single_setup(int64_t* offsets1, int32_t* order, int32_t* counts, int* queues, int n) {
   offsets1[0] = 0;
   offsets1[1] = n;
@@ -319,6 +372,7 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, const
   const int b = bucket_of(n);
   if (b < 0 && (!sc.large_ws || n > sc.large_ws_particles || n > kLargeMaxN)) return cudaErrorInvalidValue;
   k_single_setup<<<1, 1, 0, stream>>>(sc.offsets1, sc.order, sc.counts, sc.queues, n);
+  k_check_single<<<1, 256, 0, stream>>>(base.p4, base.p4_stride, n, sc.counts, base.n_jets, sc.status);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   BatchArgs A = base;

@@ -199,3 +199,37 @@ def test_host_entry_preallocated_outputs(ctx):
         ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, out={"jets": np.zeros((total, 4), np.float32)})
     with pytest.raises(ValueError):
         ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, out={"n_jets": np.zeros(b.n_events - 1, np.int32)})
+
+
+def test_non_finite_momenta_are_refused(ctx):
+    """An event with a NaN or infinite momentum component is refused on the
+    device (no jets, FJG_EINVAL); the other events of the batch are clustered
+    as usual.  The same for the one-event path."""
+    import torch
+    import fastjet_gpu_gb300 as F
+    b = E.mixed_batch(12, 20, 600, seed=61)
+    clean = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4, history=True)
+    bad_p = b.particles.copy()
+    bad_p[b.offsets[3] + 1, 2] = np.nan
+    bad_p[b.offsets[7], 3] = np.inf
+    with pytest.raises(F.FjgError):
+        ctx.cluster_batch(bad_p, b.offsets, -1, 0.4)
+    p4 = torch.from_numpy(bad_p).cuda()
+    off = torch.from_numpy(b.offsets).cuda()
+    out = ctx.cluster_batch_device(p4, off, -1, 0.4, history=True)
+    torch.cuda.synchronize()
+    with pytest.raises(F.FjgError):
+        ctx.check()
+    nj = out["n_jets"].cpu().numpy()
+    jets = out["jets"].cpu().numpy()
+    assert nj[3] == 0 and nj[7] == 0
+    for e in range(b.n_events):
+        if e in (3, 7):
+            continue
+        o = b.offsets[e]
+        assert nj[e] == clean["n_jets"][e]
+        assert np.array_equal(jets[o:o + nj[e]], clean["jets"][o:o + nj[e]])
+    one = torch.from_numpy(bad_p[b.offsets[3]:b.offsets[4]].copy()).cuda()
+    with pytest.raises(F.FjgError):
+        ctx.cluster_event(one, -1, 0.4)
+    ctx.cluster_batch(b.particles, b.offsets, -1, 0.4)  # the context stays usable
