@@ -138,3 +138,14 @@ def test_pileup_workload_properties(ctx):
         alone = _one(ctx, b.event(1), algo, radius)
         o0, o1 = b.offsets[1], b.offsets[2]
         assert np.array_equal(alone["history"], r1["history"][o0:o1])
+
+
+def test_very_large_event_properties(ctx):
+    """One 100k-particle event (beyond the 10k-60k workload): complete history,
+    every jet the sum of its constituents, identical when run twice."""
+    ev = _pileup(100000, 40, axes=6)
+    r1 = _one(ctx, ev, -1, 0.4)
+    r2 = _one(ctx, ev, -1, 0.4)
+    for k in ("jets", "jet_label", "n_jets", "history", "owner"):
+        assert np.array_equal(r1[k], r2[k]), k
+    _properties(ev, r1, 0, r1["n_jets"][0], "100k")
