@@ -69,7 +69,8 @@ typedef struct {
 
 /* Outputs of a batch, CSR-indexed by the batch's offsets (event e owns
  * [offsets[e], offsets[e+1])).  Jets of event e are jets[offsets[e] + k],
- * k < n_jets[e], in promotion order.  history and owner may be NULL. */
+ * k < n_jets[e], in promotion order; rows of jets and jet_label past
+ * n_jets[e] are left unspecified (not cleared).  history and owner may be NULL. */
 typedef struct {
   double* jets;       /* [total][4] px, py, pz, E */
   int32_t* jet_label; /* [total] label of each jet */

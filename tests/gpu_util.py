@@ -41,3 +41,16 @@ def compare_event(p4, algo, radius, jets, n_jets, history=None, owner=None, jet_
     if owner is not None:
         assert np.array_equal(owner, ref.owner), f"{ctx}: constituents differ"
     return ref
+
+
+def same_results(r1, r2, offsets, keys=("n_jets", "history", "owner")):
+    """Two runs agree on every defined output: the whole of `keys` (those
+    present), and the first n_jets[e] rows of jets and jet_label per event
+    (rows past n_jets[e] are unspecified)."""
+    for k in keys:
+        if k in r1 or k in r2:
+            assert np.array_equal(r1[k], r2[k]), k
+    for e in range(len(offsets) - 1):
+        o, nj = int(offsets[e]), int(r1["n_jets"][e])
+        for k in ("jets", "jet_label"):
+            assert np.array_equal(r1[k][o:o + nj], r2[k][o:o + nj]), (k, e)
