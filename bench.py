@@ -61,7 +61,7 @@ WORKLOADS["serving"] = dict(
 SERVING_RATES = (2000, 4000, 20000, 50000, 100000, 200000)  # the first two below capacity
 # DRAM bytes per particle of a shared-memory clustering launch (read + write),
 # from the ncu capture summarised in profiles/cluster_smem_mixed_full.md
-TRAFFIC_B_PER_PARTICLE = 58.7
+TRAFFIC_B_PER_PARTICLE = 55.9  # 59.9 MB for 1,071,102 particles
 # the same for the tiled kernel (profiles/cluster_tiled_pileup2_sections.md:
 # 5.0 MB of DRAM traffic for 103,475 particles)
 TRAFFIC_TILED_B_PER_PARTICLE = 48.3
