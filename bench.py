@@ -466,6 +466,7 @@ def run_serving(args, rank, world, local_rank):
         srv.replay(batch.particles[: batch.offsets[k]], batch.offsets[: k + 1], algo[:k], radius[:k],
                    np.arange(k) * 50.0)
     rates = []
+    launches0 = srv.launches
     with ClockSampler(local_rank) as clk:
         for rate in SERVING_RATES:
             arrival = np.cumsum(gaps) * (1e6 / rate)
@@ -474,6 +475,7 @@ def run_serving(args, rank, world, local_rank):
                           "p50_ms": float(np.percentile(lat, 50)) / 1e3, "p99_ms": float(np.percentile(lat, 99)) / 1e3,
                           "p50_ms_le2000": float(np.percentile(lat[small], 50)) / 1e3,
                           "p99_ms_le2000": float(np.percentile(lat[small], 99)) / 1e3})
+    launches = srv.launches - launches0
     # lightly loaded: requests one at a time (latency of a lone event)
     lone_idx = np.linspace(0, N_EVENTS - 1, 64).astype(int)
     lone = []
@@ -522,7 +524,7 @@ def run_serving(args, rank, world, local_rank):
             "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
             "e2e": {"value": top["served"], "unit": "events/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 0},
-            "gpu_launches": None, "clocks": clk.summary()}
+            "gpu_launches": launches, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     ctx.close()
 

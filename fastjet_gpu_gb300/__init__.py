@@ -133,6 +133,8 @@ def lib():
         L.fjg_server_poll.argtypes = [P, ctypes.POINTER(_Served), I, ctypes.POINTER(I), ctypes.c_int64]
         L.fjg_server_release.argtypes = [P, ctypes.c_uint64]
         L.fjg_server_pending.argtypes = [P]
+        L.fjg_server_launches.argtypes = [P]
+        L.fjg_server_launches.restype = ctypes.c_int64
         L.fjg_server_replay.argtypes = [P, P, P, I, P, P, P, P, ctypes.POINTER(D)]
         i64p = ctypes.POINTER(ctypes.c_int64)
         L.fjg_parse_events.argtypes = [P, ctypes.c_size_t, I, P, ctypes.c_int64, P, ctypes.c_int64, i64p, i64p, i64p]
@@ -509,6 +511,11 @@ class Server:
     @property
     def pending(self):
         return lib().fjg_server_pending(self._h)
+
+    @property
+    def launches(self):
+        """Clustering kernels launched so far (one per micro-batch)."""
+        return int(lib().fjg_server_launches(self._h))
 
     def replay(self, particles, offsets, algo, radius, arrival_us):
         """Open-loop replay of a trace; returns (latency_us per event, wall_us)."""

@@ -117,6 +117,7 @@ struct fjg_server {
   int limit[fjg::kNumQueues] = {};
   uint64_t next_ticket = 1;
   int outstanding = 0;  // submitted, not yet returned by poll
+  int64_t launches = 0;  // clustering kernels launched (inputs are checked on the host at submission)
   bool failed = false;
 };
 
@@ -210,6 +211,7 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
     const int per_sm = fjg::bucket_per_sm(ctx->tune, q);
     err = fjg::launch_variant(ctx->tune.bucket[q].variant, A, std::min(m, ctx->num_sms * per_sm), per_sm, L.stream);
   }
+  if (err == cudaSuccess) ++S->launches;
   if (err == cudaSuccess) err = cudaMemcpyAsync(L.h_status, L.d_status, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
   if (err == cudaSuccess) err = cudaEventRecord(L.ev, L.stream);
   L.busy = true;
@@ -516,6 +518,8 @@ fjg_status fjg_server_release(fjg_server* S, uint64_t ticket) {
 }
 
 int fjg_server_pending(const fjg_server* S) { return S ? S->outstanding : 0; }
+
+int64_t fjg_server_launches(const fjg_server* S) { return S ? S->launches : 0; }
 
 fjg_status fjg_server_replay(fjg_server* S, const double* p4, const int64_t* offsets, int n_events,
                              const int32_t* algo, const double* radius, const double* arrival_us,

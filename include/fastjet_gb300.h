@@ -290,6 +290,8 @@ fjg_status fjg_server_poll(fjg_server* server, fjg_served* out, int max, int* n_
 fjg_status fjg_server_release(fjg_server* server, uint64_t ticket);
 /* Submitted and not yet returned by fjg_server_poll. */
 int fjg_server_pending(const fjg_server* server);
+/* Clustering kernels launched by the server so far (one per micro-batch). */
+int64_t fjg_server_launches(const fjg_server* server);
 /* Open-loop replay of a request trace (benchmarking): event i (CSR p4 and
  * offsets in host memory, algo[i], radius[i]) is submitted at arrival_us[i]
  * microseconds after the start, results are released as they complete, and

@@ -121,6 +121,8 @@ def test_server_replay_open_loop(ctx):
     try:
         lat, wall = srv.replay(batch.particles, batch.offsets, algo, radius, arrival)
         assert srv.pending == 0
+        # continuous batching: at least one launch, at most one per request
+        assert 1 <= srv.launches <= batch.n_events
     finally:
         srv.close()
     assert lat.shape == (batch.n_events,) and np.all(lat > 0)
