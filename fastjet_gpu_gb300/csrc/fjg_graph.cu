@@ -36,6 +36,7 @@ fjg_status fjg_graph_capture_batch(fjg_ctx* ctx, const double* p4, const int64_t
   if (err == cudaSuccess) err = g->scratch.reserve_large(total);
   // resolve the per-device launch attributes and occupancies outside the capture
   for (int b = 0; b < fjg::kNumBuckets && err == cudaSuccess; ++b) fjg::variant_occupancy(ctx->tune.bucket[b].variant);
+  if (err == cudaSuccess) err = fjg::configure_tiled();
   fjg::launch_priority(0);
   if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
   if (err != cudaSuccess) {

@@ -39,7 +39,24 @@ int launch_priority(int level) {
   return p > least ? least : p;
 }
 
+// The tiled kernel keeps its state in global memory and leans on L1 (it has
+// 3.8 KB of shared memory): ask for the largest L1 split, so that it does not
+// run with the small L1 that the shared-memory bucket kernels leave on an SM.
+cudaError_t configure_tiled() {
+  static bool done[64] = {};
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+  err = cudaFuncSetAttribute(k_cluster_tiled, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxL1);
+  if (err == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+  return err;
+}
+
 cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
+  cudaError_t err = configure_tiled();
+  if (err != cudaSuccess) return err;
   return launch_with_priority(k_cluster_tiled, grid, kTiledT, 0, s, tiled_priority_level(A.serve_order), A);
 }
 
@@ -225,6 +242,8 @@ static cudaError_t launch_large(const BatchArgs& base, const Scratch& sc, int n_
   int grid = tune.large_ctas_per_sm * num_sms;
   if (grid > n_events) grid = n_events;
   if (grid < 1) grid = 1;
+  cudaError_t err = configure_tiled();
+  if (err != cudaSuccess) return err;
   k_cluster_tiled<<<grid, kTiledT, 0, s>>>(A);
   return cudaGetLastError();
 }
@@ -385,6 +404,7 @@ cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, const
   if (b < 0) {
     A.large_ws = sc.large_ws;
     A.tile_factor = tune.tile_factor;
+    if ((err = configure_tiled()) != cudaSuccess) return err;
     k_cluster_tiled<<<1, kTiledT, 0, stream>>>(A);
     return cudaGetLastError();
   }

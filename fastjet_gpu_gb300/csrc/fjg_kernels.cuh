@@ -97,6 +97,8 @@ cudaError_t launch_with_priority(K kernel, int grid, int threads, size_t smem, c
 
 // The tiled kernel over the work list of A (a persistent grid of `grid` CTAs).
 cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s);
+// Sets the tiled kernel's launch attributes once per device (outside a capture).
+cudaError_t configure_tiled();
 
 // Launch variant v (a persistent grid of `grid` CTAs); resident CTAs per SM of
 // variant v on the current device.
