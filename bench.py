@@ -63,8 +63,8 @@ SERVING_RATES = (2000, 4000, 20000, 50000, 100000, 200000)  # the first two belo
 # from the ncu capture summarised in profiles/cluster_smem_mixed_full.md
 TRAFFIC_B_PER_PARTICLE = 55.9  # 59.9 MB for 1,071,102 particles
 # the same for the tiled kernel (profiles/cluster_tiled_pileup2_sections.md:
-# 5.0 MB of DRAM traffic for 103,475 particles)
-TRAFFIC_TILED_B_PER_PARTICLE = 48.3
+# 4.8 MB of DRAM traffic for 103,475 particles)
+TRAFFIC_TILED_B_PER_PARTICLE = 46.4
 W = WORKLOADS["mixed"]
 N_EVENTS = W["events"]
 METRIC = W["metric"]
