@@ -75,6 +75,7 @@ class _Tuning(ctypes.Structure):
 
 
 FJG_TUNE_SKIP_LARGE = 1
+MAX_EVENT_PARTICLES = 1 << 24  # FJG_MAX_EVENT_PARTICLES: larger events are refused (FJG_ETOOBIG)
 FJG_SERVE_HISTORY = 1
 
 

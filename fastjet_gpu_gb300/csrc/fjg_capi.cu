@@ -10,6 +10,8 @@
 #include "fastjet_gb300.h"
 #include "fjg_context.h"
 
+static_assert(fjg::kLargeMaxN == FJG_MAX_EVENT_PARTICLES, "the C ABI states the kernels' size limit");
+
 using fjg::BatchArgs;
 
 namespace {

@@ -44,8 +44,10 @@ typedef enum {
 #define FJG_CAM 0
 #define FJG_ANTIKT (-1)
 
-/* Largest event the library clusters (particles per event). */
-#define FJG_MAX_EVENT_PARTICLES 262144
+/* Largest event the library clusters (particles per event); larger events
+ * are refused with FJG_ETOOBIG.  Events above 4096 particles also need the
+ * tiled kernel's workspace (96 bytes per particle of the batch). */
+#define FJG_MAX_EVENT_PARTICLES 16777216
 
 /* I/O record of the reference (PseudoJet.h:4-11): 40 bytes, px at offset 8. */
 typedef struct {

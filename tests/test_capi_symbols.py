@@ -57,3 +57,10 @@ def test_compat_header_matches_reference_layout():
     assert F.PSEUDOJET.itemsize == 40
     assert F.PSEUDOJET.fields["px"][1] == 8 and F.PSEUDOJET.fields["E"][1] == 32
     assert int(F.Algorithm.Kt) == 1 and int(F.Algorithm.CambridgeAachen) == 0 and int(F.Algorithm.AntiKt) == -1
+
+
+def test_size_limit_constant_matches_header():
+    import fastjet_gpu_gb300 as F
+    text = open(os.path.join(ROOT, "include", "fastjet_gb300.h")).read()
+    m = re.search(r"#define FJG_MAX_EVENT_PARTICLES (\d+)", text)
+    assert m and int(m.group(1)) == F.MAX_EVENT_PARTICLES

@@ -168,7 +168,7 @@ def test_too_big_is_reported(ctx):
     jets = torch.zeros((8, 4), dtype=torch.float64, device="cuda")
     lab = torch.zeros(8, dtype=torch.int32, device="cuda")
     nj = torch.zeros(1, dtype=torch.int32, device="cuda")
-    st = F.lib().fjg_cluster_event(ctx._h, ctypes.c_void_p(small.data_ptr()), (1 << 24) + 1, -1, 0.4,
+    st = F.lib().fjg_cluster_event(ctx._h, ctypes.c_void_p(small.data_ptr()), F.MAX_EVENT_PARTICLES + 1, -1, 0.4,
                                    ctypes.c_void_p(jets.data_ptr()), ctypes.c_void_p(lab.data_ptr()),
                                    ctypes.c_void_p(nj.data_ptr()), None, None)
     assert st == 4
