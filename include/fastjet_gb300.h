@@ -185,10 +185,11 @@ void fjg_graph_destroy(fjg_graph* graph);
  * 256, 512, 1024, 2048 and 4096 particles (buckets 0-4) with one of several
  * compiled kernel shapes each (CTA threads x slots per thread = the bucket's
  * capacity) and a persistent grid of ctas_per_sm CTAs per SM (0: as many as
- * fit); events above 4096 particles run on the tiled kernel with
- * large_ctas_per_sm CTAs per SM and rapidity-azimuth tiles of side
- * tile_factor * R (>= 1).  Every choice gives identical results; only the
- * speed differs. */
+ * fit); events above 4096 particles run on the tiled kernel with a grid of
+ * large_ctas_per_sm CTAs per SM (one is resident per SM) and rapidity-azimuth
+ * tiles of side at least tile_factor * R (tile_factor >= 1), larger where an
+ * event is sparse (about 32 particles per tile).  Every choice gives identical
+ * results; only the speed differs. */
 #define FJG_NUM_BUCKETS 5
 typedef struct {
   int32_t threads[FJG_NUM_BUCKETS];          /* CTA size: 64 .. 512 */
