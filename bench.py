@@ -45,7 +45,7 @@ WORKLOADS = {
         metric="events/s, batched anti-kt R=0.4 clustering of 4096 events (50-2000 particles)",
         workload="4096 events, particle counts log-uniform in [50, 2000], anti-kt R=0.4, FP64, one batched call"),
     "pileup": dict(
-        events=64, make=lambda n: E.pileup_batch(n, 10000, 60000, seed=4), flush=False, cpu_start=16,
+        events=64, make=lambda n: E.pileup_batch(n, 10000, 60000, seed=4), flush=True, cpu_start=16,
         per_event_sample=4, second=(1, 0.6), dominant=None,
         metric="events/s, batched anti-kt R=0.4 clustering of 64 pile-up events (10k-60k particles)",
         workload="64 pile-up-like events, 10k-60k particles, anti-kt R=0.4 (kt R=0.6 beside it), FP64, "
@@ -266,7 +266,7 @@ def run_ours(args, rank, world, local_rank):
         with torch.cuda.stream(stream):  # the library's stream: its kernels, the flush and the events
             for k in range(k_steps):
                 if W["flush"]:
-                    flush.fill_(float(k))  # evict L2 between steps (inputs are ~70 MB < 129 MB L2)
+                    flush.fill_(float(k))  # evict L2 between steps (the inputs, 70-80 MB, fit in the 129 MB L2)
                 torch.cuda.nvtx.range_push("timed_step")
                 starts[k].record(stream)
                 step(algo, radius)
@@ -403,8 +403,7 @@ def run_ours(args, rank, world, local_rank):
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * step_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "events": N_EVENTS, "particles": total, "algorithm": "anti-kt",
-                       "R": RADIUS, "l2": ("flushed between steps (256 MiB write)" if W["flush"] else
-                                           "not flushed: a step runs for a second or more"),
+                       "R": RADIUS, "l2": "flushed between steps (256 MiB write)" if W["flush"] else "not flushed",
                        "parallelism": f"replicas{world}", "cuda_graph": graph is not None,
                        "tuning": tuning},
             "per_event_launch": per_event,
@@ -515,6 +514,7 @@ def run_serving(args, rank, world, local_rank):
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * float(np.mean([r["wall_s"] for r in rates])),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "requests_per_rate": N_EVENTS, "particles": int(batch.offsets[-1]),
+                       "l2": "not flushed: each request's momenta are copied in from host memory as it arrives",
                        "rates": rates, "tuning": tuning,
                        "lone_request_ms": {"p50": float(np.percentile(lone, 50)), "p99": float(np.percentile(lone, 99)),
                                            "p50_le2000": float(np.percentile(lone_small, 50)),
