@@ -64,3 +64,19 @@ def test_size_limit_constant_matches_header():
     text = open(os.path.join(ROOT, "include", "fastjet_gb300.h")).read()
     m = re.search(r"#define FJG_MAX_EVENT_PARTICLES (\d+)", text)
     assert m and int(m.group(1)) == F.MAX_EVENT_PARTICLES
+
+
+def test_host_side_argument_checks():
+    """Calls refused before any device work: a null context, a null server,
+    and (without a GPU) context creation reports a CUDA error, not a crash."""
+    import fastjet_gpu_gb300 as F
+    L = F.lib()
+    st = L.fjg_cluster_batch(None, None, None, 1, 0, None, -1, None, 0.4, None, None)
+    assert st == 1 and b"ctx is null" in L.fjg_last_error(None)
+    assert L.fjg_server_pending(None) == 0 and L.fjg_server_launches(None) == 0
+    import torch
+    if not torch.cuda.is_available():
+        h = ctypes.c_void_p()
+        st = L.fjg_ctx_create(0, ctypes.byref(h))
+        assert st != 0 and not h.value
+        assert L.fjg_last_error(None)
