@@ -122,6 +122,143 @@ def pileup_batch(n_events=64, lo=10000, hi=60000, seed=4):
                         for n, a, s in zip(sizes, axes, seeds)])
 
 
+# ------------------------------------------------- bit-reproducible generator
+#
+# The generators above call numpy's distributions and libm (cos, sinh, log),
+# whose last bits differ between hosts (x86 and Arm here), so events they make
+# are committed as consumed.  The one below uses only the raw 64-bit words of
+# PCG64 and correctly rounded IEEE operations (+, -, *, /, sqrt, frexp/ldexp,
+# rint), each a separate numpy ufunc or Python float operation, so it yields
+# the same bits on every host: large events can be regenerated instead of
+# committed.  Its logarithm, exponential and sine/cosine are short series,
+# accurate to a few ulp -- only their determinism matters.
+
+_LN2 = 0.6931471805599453
+_SQRT_HALF = 0.7071067811865476
+
+
+def _p_uniform(bitgen, n):
+    """n doubles in [0, 1): the top 53 bits of each raw PCG64 word."""
+    raw = bitgen.random_raw(n)
+    return (raw >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def _p_log(x):
+    """Natural logarithm of positive x: 2 atanh((m-1)/(m+1)) + e ln2."""
+    m, e = np.frexp(x)
+    low = m < _SQRT_HALF
+    m = np.where(low, m * 2.0, m)
+    e = np.where(low, e - 1, e).astype(np.float64)
+    s = (m - 1.0) / (m + 1.0)
+    s2 = s * s
+    acc = np.full_like(s, 1.0 / 31.0)
+    for k in range(14, -1, -1):
+        acc = acc * s2 + 1.0 / (2 * k + 1)
+    return (2.0 * s) * acc + e * _LN2
+
+
+def _p_exp(x):
+    """exp(x) for |x| < 700: x = k ln2 + r, Taylor series of r, scaled by 2^k."""
+    k = np.rint(x / _LN2)
+    r = x - k * _LN2
+    acc = np.full_like(r, 1.0)
+    for j in range(24, 0, -1):
+        acc = acc * (r / j) + 1.0
+    return np.ldexp(acc, k.astype(np.int64))
+
+
+def _p_sincos(a):
+    """(sin a, cos a) for |a| <= 4: series at a/4, then two angle doublings."""
+    q = a * 0.25
+    q2 = q * q
+    s = np.full_like(q, 0.0)
+    c = np.full_like(q, 0.0)
+    for j in range(12, -1, -1):
+        s = s * q2 * (-1.0 / ((2 * j + 2) * (2 * j + 3))) + 1.0
+        c = c * q2 * (-1.0 / ((2 * j + 1) * (2 * j + 2))) + 1.0
+    s = s * q
+    for _ in range(2):
+        s, c = 2.0 * s * c, c * c - s * s
+    return s, c
+
+
+def _p_gauss(bitgen, n, sigma):
+    """Gaussian(0, sigma) by Box-Muller on the functions above."""
+    u1 = 1.0 - _p_uniform(bitgen, n)  # (0, 1]
+    u2 = _p_uniform(bitgen, n)
+    rad = np.sqrt(-2.0 * _p_log(u1))
+    _, c = _p_sincos((u2 - 0.5) * (2.0 * math.pi))
+    return sigma * rad * c
+
+
+def portable_event(n, n_axes, seed, soft_mean=0.6, soft_eta=4.0, eta_span=2.5):
+    """One event of exactly ``n`` massless particles, float64 [n, 4], with the
+    same bits on every host.
+
+    Hard axes: axis pT = 30 GeV * u^(-1/3) (a 1/pT^4 spectrum above 30 GeV),
+    eta U[-eta_span, eta_span], phi U[-pi, pi); 10-20 constituents with
+    momentum fractions from normalised Exp(1) draws (Dirichlet(1)) and
+    Gaussian sigma=0.1 offsets in eta and phi.  Soft background: pT
+    Exp(soft_mean) floored at 0.1 GeV, eta U[-soft_eta, soft_eta], phi
+    U[-pi, pi).  E = |p|.  Particles are in a seeded random order.
+    """
+    bg = np.random.PCG64(seed)
+    pts, etas, phis = [], [], []
+    room = n
+    for _ in range(n_axes):
+        u = _p_uniform(bg, 4)
+        axis_pt = float(30.0 * _p_exp(_p_log(1.0 - u[0:1]) * (-1.0 / 3.0))[0])
+        axis_eta = float(eta_span * (2.0 * u[1] - 1.0))
+        axis_phi = float(math.pi * (2.0 * u[2] - 1.0))
+        k = min(10 + int(u[3] * 11.0), room)
+        if k <= 0:
+            continue
+        x = -_p_log(1.0 - _p_uniform(bg, k))
+        tot = 0.0
+        for v in x.tolist():
+            tot += v
+        pts.append(axis_pt * (x / tot))
+        etas.append(axis_eta + _p_gauss(bg, k, 0.1))
+        phis.append(axis_phi + _p_gauss(bg, k, 0.1))
+        room -= k
+    n_soft = room
+    pt_s = np.maximum(-soft_mean * _p_log(1.0 - _p_uniform(bg, n_soft)), 0.1)
+    eta_s = soft_eta * (2.0 * _p_uniform(bg, n_soft) - 1.0)
+    phi_s = math.pi * (2.0 * _p_uniform(bg, n_soft) - 1.0)
+    pt = np.concatenate(pts + [pt_s])
+    eta = np.concatenate(etas + [eta_s])
+    phi = np.concatenate(phis + [phi_s])
+    # azimuth: reduce to [-pi, pi] (constituents may sit past the edge)
+    phi = np.where(phi > math.pi, phi - 2.0 * math.pi, np.where(phi < -math.pi, phi + 2.0 * math.pi, phi))
+    sn, cs = _p_sincos(phi)
+    ep = _p_exp(eta)
+    em = 1.0 / ep
+    px = pt * cs
+    py = pt * sn
+    pz = pt * ((ep - em) * 0.5)
+    E = np.sqrt(px * px + py * py + pz * pz)
+    # seeded permutation: sort by raw words (distinct with overwhelming odds)
+    order = np.argsort(bg.random_raw(n), kind="stable")
+    return np.ascontiguousarray(np.stack([px, py, pz, E], axis=1)[order])
+
+
+def portable_pileup(sizes, seed=40, n_axes=(2, 6)):
+    """Pile-up-like events of the given sizes (portable_event, 2-6 hard axes)."""
+    bg = np.random.PCG64(seed)
+    raw = bg.random_raw(2 * len(sizes))
+    evs = []
+    for i, n in enumerate(sizes):
+        axes = n_axes[0] + int(raw[2 * i] % np.uint64(n_axes[1] - n_axes[0] + 1))
+        evs.append(portable_event(int(n), axes, int(raw[2 * i + 1] >> np.uint64(1))))
+    return evs
+
+
+def event_sha256(p4):
+    """SHA-256 of an event's float64 [n, 4] array (little-endian bytes)."""
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(p4, dtype="<f8").tobytes()).hexdigest()
+
+
 ALGO_KT, ALGO_CAM, ALGO_ANTIKT = 1, 0, -1
 
 

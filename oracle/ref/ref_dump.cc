@@ -7,7 +7,11 @@
 // is copied to a device buffer, cluster() rewrites it in place, the buffer is
 // copied back.  Every output slot is printed as
 //   slot index isJet px py pz E        (momenta as C99 hex floats, exact)
-// one line per slot, and each event ends with a line "end <N>".
+// one line per slot, and each event ends with a line "end <N>".  Linked with
+// the history-printing copy of a backend (stage_hist.py), the backend's own
+// device printf adds one "H ..." line per clustering step before the slots; the
+// printf FIFO is enlarged for that, as the reference driver does (main.cc:28),
+// and stdout is flushed around every event so the lines stay in event order.
 //
 // usage: <backend>_dump (-kt|-antikt|-cam) R < events.txt
 // Input: the reference's text format (px py pz E per line, events separated by
@@ -54,6 +58,11 @@ int main(int argc, char** argv) {
   else if (!std::strcmp(argv[1], "-cam")) algo = Algorithm::CambridgeAachen;
   else { std::fprintf(stderr, "bad algorithm %s\n", argv[1]); return 2; }
   double r = std::strtod(argv[2], nullptr);
+  // one step line takes ~200 bytes of the FIFO; room for events of ~1M particles
+  if (cudaDeviceSetLimit(cudaLimitPrintfFifoSize, (size_t)256 << 20) != cudaSuccess) {
+    std::fprintf(stderr, "cannot size the printf FIFO\n");
+    return 1;
+  }
 
   std::vector<PseudoJet> ev;
   while (read_event(std::cin, ev)) {
@@ -61,6 +70,7 @@ int main(int argc, char** argv) {
     size_t bytes = sizeof(PseudoJet) * ev.size();
     if (cudaMalloc(&d, bytes) != cudaSuccess) { std::fprintf(stderr, "cudaMalloc failed\n"); return 1; }
     cudaMemcpy(d, ev.data(), bytes, cudaMemcpyDefault);
+    std::fflush(stdout);
     cluster(d, (int)ev.size(), algo, r);
     cudaMemcpy(ev.data(), d, bytes, cudaMemcpyDefault);
     cudaError_t err = cudaDeviceSynchronize();
@@ -71,6 +81,7 @@ int main(int argc, char** argv) {
       std::printf("%zu %d %d %a %a %a %a\n", s, p.index, p.isJet ? 1 : 0, p.px, p.py, p.pz, p.E);
     }
     std::printf("end %zu\n", ev.size());
+    std::fflush(stdout);
   }
   return 0;
 }

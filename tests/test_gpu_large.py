@@ -1,9 +1,12 @@
 """Events above 4096 particles (the tiled kernel) vs the CPU oracle (needs a GB300).
 
-Sizes up to 20k particles are checked against the portable-kinematics oracle
-bit for bit (merge history with distances, jets, constituents).  The 10k-60k
-pile-up workload itself is too slow for the O(N^2) oracle; there the checks
-are size-independent properties: momentum conservation per jet from the
+Events up to 20k particles, and three at the pile-up workload's sizes (31k,
+45k and 60k particles, the oracle on one host thread per event), are checked
+against the portable-kinematics oracle bit for bit (merge history with
+distances, jets, constituents).  The reference's own grid backend is checked
+on 10k-22k-particle events in test_gpu_parity (jets and merge histories).  The
+whole 64-event workload and a 100k-particle event are checked through
+size-independent properties: momentum conservation per jet from the
 constituent map, a complete history, and identical results alone, in a batch
 and run twice.
 """
@@ -147,3 +150,25 @@ def test_very_large_event_properties(ctx):
     r2 = _one(ctx, ev, -1, 0.4)
     U.same_results(r1, r2, [0, ev.shape[0]])
     _properties(ev, r1, 0, r1["n_jets"][0], "100k")
+
+
+def test_workload_size_events_match_oracle(ctx):
+    """Pile-up-like events at the workload's sizes (31k, 45k and 60k
+    particles), anti-kt R=0.4 and kt R=0.6: merge history, jets, labels and
+    constituents identical bit for bit to the oracle (portable kinematics),
+    which clusters the three events on three host threads."""
+    import oracle
+    evs = E.portable_pileup([31000, 45000, 60000], seed=41)
+    b = E._batch_from(evs)
+    for algo, radius in ((-1, 0.4), (1, 0.6)):
+        res = ctx.cluster_batch(b.particles, b.offsets, algo, radius, history=True, owner=True)
+        hist, jets, lab, own, nj, _ = oracle.cluster_batch(b.particles, b.offsets, algo, radius, threads=3,
+                                                           portable=True)
+        assert np.array_equal(res["n_jets"], nj)
+        assert np.array_equal(res["history"]["a"], hist["a"]) and np.array_equal(res["history"]["b"], hist["b"])
+        assert np.array_equal(res["history"]["d"], hist["d"])
+        assert np.array_equal(res["owner"], own)
+        for e in range(b.n_events):
+            o = b.offsets[e]
+            assert np.array_equal(res["jets"][o:o + nj[e]], jets[o:o + nj[e]]), (algo, e)
+            assert np.array_equal(res["jet_label"][o:o + nj[e]], lab[o:o + nj[e]]), (algo, e)

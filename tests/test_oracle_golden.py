@@ -3,15 +3,19 @@
 Goldens: tests/golden/make_golden.py ran the reference's tri_matrix, grid and
 n_array backends (built from the reference sources) on the reference fixtures
 and on seeded synthetic events, for kt / C-A / anti-kt and R in {0.4, 0.6,
-0.8, 1.0}; all backends agreed on every case.
+0.8, 1.0}; all backends agreed on every case.  The grid backend also ran on
+pile-up-like events of 10k-22k particles (anti-kt R=0.4, kt R=0.6), and
+history-printing copies of tri_matrix and grid recorded every merge step.
 """
 import collections
+import os
 
 import numpy as np
 import pytest
 
 import oracle
 import golden_util as G
+from fastjet_gpu_gb300 import events as E
 
 
 def test_full_jets_match_reference():
@@ -28,18 +32,64 @@ def test_full_jets_match_reference():
 
 
 def test_all_digests_match_reference():
-    by_input = collections.defaultdict(list)
+    """Every reference case: the 552 of the fixtures and synthetic inputs (all
+    backends agreeing) and the large pile-up-like events (the grid backend)."""
+    by = collections.defaultdict(list)
     for case in G.cases():
-        by_input[case[0]].append(case)
+        by[(case[0], case[1], case[2])].append(case)
     n = 0
-    for name, cs in by_input.items():
-        evs = G.inputs(name)
-        for _, algo, radius, ev, nj, dg in cs:
-            res = oracle.cluster(evs[ev], G.ALGO_CODE[algo], float(radius))
-            assert len(res.jets) == nj, (name, algo, radius, ev)
-            assert G.jets_digest(res.jets) == dg, (name, algo, radius, ev)
+    for (name, algo, radius), cs in sorted(by.items()):
+        evs = G.golden_events(name)
+        b = E._batch_from(evs)
+        _, jets, _, _, n_jets, _ = oracle.cluster_batch(b.particles, b.offsets, G.ALGO_CODE[algo], float(radius),
+                                                        threads=os.cpu_count() or 4, want_history=False)
+        for _, _, _, ev, nj, dg in cs:
+            o = b.offsets[ev]
+            assert n_jets[ev] == nj, (name, algo, radius, ev)
+            assert G.jets_digest(jets[o:o + nj]) == dg, (name, algo, radius, ev)
             n += 1
-    assert n == 552
+    assert n == 552 + 8
+
+
+def test_large_inputs_regenerate_bit_for_bit():
+    """The large golden events come from events.portable_pileup, which uses
+    only correctly rounded operations: they regenerate with the SHA-256 of the
+    events the reference read (on the GPU host, another architecture)."""
+    evs = G.large_inputs("pileup4")
+    assert [ev.shape[0] for ev in evs] == [10000, 13000, 17000, 22000]
+
+
+def test_oracle_matches_reference_histories():
+    """The reference's own merge histories (tri_matrix and grid, printed by
+    their commented-out step printfs, tri_matrix.cu:235 and grid.cu:454,462,
+    enabled in a copy; tests/golden/make_golden.py): every case's sequence of
+    merged pairs and promotions is the oracle's, up to the order of steps
+    inside ties and near ties (distances equal within 1e-12 relative: the
+    reference's FMA-contracted pt^2 of particles of equal pT), and the
+    rebuilt sequence hashes to the reference's."""
+    cases = G.history_cases()
+    groups = collections.defaultdict(list)
+    for key in cases:
+        name, backend, algo, radius = key.split(".", 3)
+        groups[(name, algo, radius)].append(key)
+    checked = 0
+    for (name, algo, radius), keys in sorted(groups.items()):
+        evs = G.golden_events(name)
+        b = E._batch_from(evs)
+        hist = oracle.cluster_batch(b.particles, b.offsets, G.ALGO_CODE[algo], float(radius),
+                                    threads=os.cpu_count() or 4, portable=True)[0]
+        for key in keys:
+            ra, rb, rd = G.reference_history(key, hist)
+            for e in range(b.n_events):
+                s0, s1 = b.offsets[e], b.offsets[e + 1]
+                k, _ = G.near_tie_mismatch(hist["a"][s0:s1], hist["b"][s0:s1], hist["d"][s0:s1], ra[s0:s1],
+                                           rb[s0:s1], rd[s0:s1])
+                assert k < 0, f"{key} event {e}: merge sequence differs at step {k}"
+            # distances: the reference's FMA-contracted FP64 and CUDA libm
+            # against correctly rounded, uncontracted FP64 (see compare_event)
+            np.testing.assert_allclose(rd, hist["d"], rtol=1e-8, atol=0, err_msg=key)
+            checked += 1
+    assert checked == len(cases) and checked >= 170
 
 
 def test_makefile_run_matrix_jet_counts():
