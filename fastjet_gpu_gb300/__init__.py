@@ -22,7 +22,9 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_lib", "libfastjet_gb300.so")
+# FJG_LIB selects another build of the library (e.g. the phase-counter build
+# in _lib_phases/, see fastjet_gpu_gb300.phases)
+LIB_PATH = os.environ.get("FJG_LIB") or os.path.join(_HERE, "_lib", "libfastjet_gb300.so")
 
 
 class Algorithm(enum.IntEnum):
@@ -77,6 +79,7 @@ class _Tuning(ctypes.Structure):
 FJG_TUNE_SKIP_LARGE = 1
 MAX_EVENT_PARTICLES = 1 << 24  # FJG_MAX_EVENT_PARTICLES: larger events are refused (FJG_ETOOBIG)
 FJG_SERVE_HISTORY = 1
+FJG_SERVE_DEVICE_CHECK = 2
 
 
 class _ServerConfig(ctypes.Structure):
@@ -109,6 +112,7 @@ def lib():
         L.fjg_ctx_check.argtypes = [P]
         L.fjg_last_error.argtypes = [P]
         L.fjg_last_error.restype = ctypes.c_char_p
+        L.fjg_phase_clocks.argtypes = [P, P, I, I]
         L.fjg_status_string.argtypes = [I]
         L.fjg_status_string.restype = ctypes.c_char_p
         L.fjg_cluster_batch.argtypes = [P, P, P, I, ctypes.c_int64, P, I, P, D, ctypes.POINTER(_Outputs), P]
@@ -225,6 +229,17 @@ class Context:
 
     def check(self):
         self._check(lib().fjg_ctx_check(self._h))
+
+    PHASES = ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
+              "rescan_s2", "steps", "events")
+
+    def phase_clocks(self, reset=False):
+        """Per-step phase counters of the shared-memory kernel (only in the
+        -DFJG_PHASE_CLOCKS build, see fastjet_gpu_gb300.phases): a dict of
+        summed clock cycles per phase, steps and events."""
+        buf = (ctypes.c_ulonglong * 16)()
+        self._check(lib().fjg_phase_clocks(self._h, buf, 16, 1 if reset else 0))
+        return {k: int(buf[i]) for i, k in enumerate(self.PHASES)}
 
     def _after_torch(self, device):
         """Make the context's stream wait for torch's current stream."""
@@ -472,10 +487,11 @@ class Server:
     poll for completed ones.  Continuous batching; see fastjet_gb300.h."""
 
     def __init__(self, ctx, arena_particles=0, max_inflight=0, streams=0, max_batch=0, oversubscribe=0,
-                 history=False):
+                 history=False, device_check=False):
         self.ctx = ctx
+        flags = (FJG_SERVE_HISTORY if history else 0) | (FJG_SERVE_DEVICE_CHECK if device_check else 0)
         cfg = _ServerConfig(int(arena_particles), int(max_inflight), int(streams), int(max_batch),
-                            int(oversubscribe), FJG_SERVE_HISTORY if history else 0)
+                            int(oversubscribe), flags)
         self._h = ctypes.c_void_p()
         ctx._check(lib().fjg_server_create(ctx._h, ctypes.byref(cfg), ctypes.byref(self._h)))
         self.history = history

@@ -68,26 +68,39 @@ def _run(cmd):
     return res
 
 
-def build(force=False, verbose=False):
-    """Compile the CUDA library and the driver; return the library path."""
-    os.makedirs(LIBDIR, exist_ok=True)
-    os.makedirs(OBJDIR, exist_ok=True)
+def build(force=False, verbose=False, phase_clocks=False):
+    """Compile the CUDA library and the driver; return the library path.
+
+    phase_clocks: a second build, with the kernels' per-step phase counters
+    compiled in (-DFJG_PHASE_CLOCKS), into _lib_phases/ (no driver); the
+    product build is unaffected.
+    """
+    libdir, objdir, lib = LIBDIR, OBJDIR, LIB
+    flags = list(NVCC_FLAGS)
+    if phase_clocks:
+        libdir, objdir = os.path.join(PKG, "_lib_phases"), os.path.join(PKG, "_build_phases")
+        lib = os.path.join(libdir, "libfastjet_gb300.so")
+        flags.append("-DFJG_PHASE_CLOCKS")
+    os.makedirs(libdir, exist_ok=True)
+    os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
     headers = _headers()
     objs, jobs = [], []
     for src in _sources():
-        obj = os.path.join(OBJDIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(objdir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([nvcc] + flags + ["-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for res in ex.map(_run, jobs):
             if verbose and res.stderr:
                 print(res.stderr, file=sys.stderr)
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + f".tmp{os.getpid()}"
+    if force or jobs or _stale(lib, objs):
+        tmp = lib + f".tmp{os.getpid()}"
         _run([nvcc, "-shared", "-o", tmp] + objs + ["-lcudart"])
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
+    if phase_clocks:
+        return lib
     drv_src = os.path.join(PKG, "driver", "fjg_cluster.cc")
     if os.path.exists(drv_src) and (force or _stale(DRIVER, [drv_src, LIB] + headers)):
         cuda = _cuda_home()
@@ -102,5 +115,6 @@ def build(force=False, verbose=False):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
+    ap.add_argument("--phase-clocks", action="store_true", help="the phase-counter build, into _lib_phases/")
     args = ap.parse_args()
-    print(build(force=args.force, verbose=True))
+    print(build(force=args.force, verbose=True, phase_clocks=args.phase_clocks))

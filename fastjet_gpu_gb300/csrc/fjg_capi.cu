@@ -148,6 +148,10 @@ fjg_status fjg_ctx_create(int device, fjg_ctx** out) {
   }
   if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
   if (err == cudaSuccess) err = ctx->scratch.reserve_lists(1024);
+#ifdef FJG_PHASE_CLOCKS
+  if (err == cudaSuccess) err = cudaMalloc(&ctx->phase, sizeof(unsigned long long) * fjg::kPhSlots);
+  if (err == cudaSuccess) err = cudaMemset(ctx->phase, 0, sizeof(unsigned long long) * fjg::kPhSlots);
+#endif
   if (err != cudaSuccess) {
     fjg_status st = cuda_error(nullptr, err, "context creation");
     fjg_ctx_destroy(ctx);
@@ -170,6 +174,7 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
   }
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->phase) cudaFree(ctx->phase);
   ctx->scratch.release();
   ctx->io.release();
   ctx->single.release();
@@ -178,6 +183,19 @@ void fjg_ctx_destroy(fjg_ctx* ctx) {
 }
 
 void* fjg_ctx_stream(fjg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+fjg_status fjg_phase_clocks(fjg_ctx* ctx, unsigned long long* out, int n, int reset) {
+  if (!ctx || (!out && n > 0)) return set_error(ctx, FJG_EINVAL, "null argument");
+  if (!ctx->phase) return set_error(ctx, FJG_EINVAL, "library built without FJG_PHASE_CLOCKS");
+  DeviceGuard g(ctx->device);
+  unsigned long long buf[fjg::kPhSlots];
+  cudaError_t err = cudaStreamSynchronize(ctx->stream);
+  if (err == cudaSuccess) err = cudaMemcpy(buf, ctx->phase, sizeof(buf), cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess && reset) err = cudaMemset(ctx->phase, 0, sizeof(buf));
+  if (err != cudaSuccess) return cuda_error(ctx, err, "phase counters");
+  for (int k = 0; k < n && k < fjg::kPhSlots; ++k) out[k] = buf[k];
+  return FJG_OK;
+}
 
 fjg_status fjg_ctx_check(fjg_ctx* ctx) {
   if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
@@ -194,7 +212,7 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   if (n_events == 0) return FJG_OK;
   if (total > 0 && (!p4 || !out->jets || !out->jet_label)) return set_error(ctx, FJG_EINVAL, "null buffer");
   if (!algo && !valid_algo(algo_all)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
-  if (!radius && !(r_all > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  if (!radius && !fjg::valid_radius(r_all)) return set_error(ctx, FJG_EINVAL, "R must be finite and >= 0");
   DeviceGuard g(ctx->device);
   cudaError_t err = ctx->scratch.reserve_lists(n_events);
   if (err == cudaSuccess) err = ctx->scratch.reserve_ws(total);
@@ -202,6 +220,7 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   if (err != cudaSuccess) return cuda_error(ctx, err, "scratch allocation");
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   BatchArgs A{};
+  A.phase = ctx->phase;
   A.p4 = p4;
   A.p4_stride = 4;
   A.offsets = offsets;
@@ -286,7 +305,7 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
   if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
   if (n < 0 || !n_jets || (n > 0 && (!p4 || !jets || !jet_label))) return set_error(ctx, FJG_EINVAL, "bad arguments");
   if (!valid_algo(algo)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
-  if (!(r > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  if (!fjg::valid_radius(r)) return set_error(ctx, FJG_EINVAL, "R must be finite and >= 0");
   DeviceGuard g(ctx->device);
   cudaStream_t s = ctx->stream;
   if (n == 0) {
@@ -299,6 +318,7 @@ fjg_status fjg_cluster_event(fjg_ctx* ctx, const double* p4, int n, int algo, do
   if (werr == cudaSuccess) werr = ctx->scratch.reserve_large(n);
   if (werr != cudaSuccess) return cuda_error(ctx, werr, "workspace allocation");
   BatchArgs A{};
+  A.phase = ctx->phase;
   A.p4 = p4;
   A.p4_stride = 4;
   A.algo = nullptr;
@@ -332,7 +352,7 @@ fjg_status fjg_cluster_pseudojets(fjg_ctx* ctx, fjg_pseudojet* particles, int si
   if (!ctx) return set_error(nullptr, FJG_EINVAL, "ctx is null");
   if (size < 0 || (size > 0 && !particles)) return set_error(ctx, FJG_EINVAL, "bad arguments");
   if (!valid_algo(algo)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
-  if (!(r > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  if (!fjg::valid_radius(r)) return set_error(ctx, FJG_EINVAL, "R must be finite and >= 0");
   if (size == 0) return FJG_OK;
   if (size > fjg::kLargeMaxN) return set_error(ctx, FJG_ETOOBIG, "event exceeds the supported particle count");
   DeviceGuard g(ctx->device);

@@ -42,6 +42,23 @@
 
 namespace fjg {
 
+// Per-step phase counters, compiled in only with -DFJG_PHASE_CLOCKS (off in
+// the product build; python -m fastjet_gpu_gb300.phases builds and reads
+// them).  Thread 0 of a CTA accumulates the clock64() time of each phase of a
+// step as it passes the phase's closing barrier (S1: argmin up to its
+// decision; S2: merge up to B2; S3: new-jet pass and targets up to B3; tail:
+// the new jet's neighbour up to the next step's start); lane 0 of each merge
+// warp the length of its kinematics chain, and the first rescan thread the
+// time of its S2 work.  At the end of an event they are added to A.phase.
+enum PhaseSlot {
+  kPhS1 = 0, kPhS2, kPhS3, kPhTail, kPhKin0, kPhKin1, kPhKin2, kPhRescan, kPhSteps, kPhEvents, kPhSlots = 16
+};
+#ifdef FJG_PHASE_CLOCKS
+#define FJG_PH(...) __VA_ARGS__
+#else
+#define FJG_PH(...)
+#endif
+
 struct StepRec {
   int32_t a, b;
   double d;
@@ -76,7 +93,13 @@ struct BatchArgs {
   int pairs;               // offsets hold (start, end) pairs: events need not be contiguous
   int* done;               // null, or completion flags: done[done_slot[e]] = 1 (system scope) per event
   const int32_t* done_slot;
+  int32_t* ev_status;      // null, or per-event status bits: an event whose word is set on entry is
+                           // skipped (refused, no jets); bits a kernel raises for event e land here too
+  unsigned long long* phase;  // [kPhSlots] phase counters (FJG_PHASE_CLOCKS builds only), or null
 };
+
+// Status bits raised by kernels (ORed into the device status word).
+enum : int { kStatusTooBig = 1, kStatusBadArg = 2, kStatusInternal = 4 };
 
 // Particle range [off, off + N) of event e.
 __device__ __forceinline__ void event_range(const BatchArgs& A, int e, int64_t& off, int& N) {
@@ -96,6 +119,27 @@ __device__ __forceinline__ void signal_done(const BatchArgs& A, int e) {
   __threadfence_system();
   int* flag = A.done + A.done_slot[e];
   asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
+}
+
+// Raise status `bit` for event e: in the batch's word and, when the caller
+// keeps per-event words (the request server), in the event's own, so that
+// only that event's request fails.
+__device__ __forceinline__ void raise_event_status(const BatchArgs& A, int e, int bit) {
+  atomicOr(A.status, bit);
+  if (A.ev_status) atomicOr(A.ev_status + e, bit);
+}
+
+// An event refused before clustering (its per-event word is set): no jets.
+// Called by every thread of the CTA after the event was fetched; ends with a
+// barrier, as the clustering routines do.
+__device__ __forceinline__ bool refused_event(const BatchArgs& A, int e) {
+  if (!A.ev_status || *(volatile int32_t*)(A.ev_status + e) == 0) return false;
+  if (threadIdx.x == 0) {
+    A.n_jets[e] = 0;
+    signal_done(A, e);
+  }
+  __syncthreads();
+  return true;
 }
 
 constexpr int kRescanChunk = 8;  // targets per register pass
@@ -444,7 +488,9 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
   // ---- clustering steps
   int n = N;
   int step = 0;
+  FJG_PH(long long ph_s1 = 0, ph_s2 = 0, ph_s3 = 0, ph_tail = 0, ph_kin = 0, ph_resc = 0, ph_b3 = 0;)
   while (n > 0) {
+    FJG_PH(const long long ph0 = clock64(); if (step > 0) ph_tail += ph0 - ph_b3;)
     // S1: argmin over (klo, label) with a certificate.  The winner's neighbour
     // and kind travel with the reduction: once B1 is passed the merge warps
     // may overwrite the winner's slot (compaction) while other warps are still
@@ -568,11 +614,12 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       __syncthreads();  // wexact, wnn, wpair may be reused in the next step
     }
     if (c < 0) {  // no candidate although n > 0: cannot happen for finite inputs
-      if (tid == 0) atomicOr(A.status, 4);
+      if (tid == 0) raise_event_status(A, e, kStatusInternal);
       break;
     }
 
     // S2: decisions every thread takes from the same values
+    FJG_PH(const long long ph1 = clock64(); ph_s1 += ph1 - ph0;)
     const bool pair = cpair != 0 && cnn >= 0;
     const int j = pair ? cnn : -1;
     const int a = pair ? min(c, j) : -1;
@@ -613,6 +660,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       }
       __syncwarp();
       if (MW > 1) named_sync(2, 32 * MW);  // every merge warp holds its inputs
+      FJG_PH(const long long pk0 = clock64();)
       const int lo_l = pair ? min(lc, lj) : lc, hi_l = max(lc, lj);
       const bool phi_role = role <= 0, rap_role = role == -1 || role == 1, w_role = role == -1 || role == 2;
       if (pair) {
@@ -653,6 +701,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
         if (A.owner) A.owner[off + lc] = -(nj + 1);
         S.ctl_njets = nj + 1;
       }
+      FJG_PH(if (lane == 0) ph_kin += clock64() - pk0;)
       if (w_role) {
         __syncwarp();
         if (b != L) move_slot_warp<T, SPT>(S, g, b, L);  // compaction (never touches slot a)
@@ -685,8 +734,10 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
         else
           rescan_chunk<8, T, SPT>(S, X, base, cnt, r0, TR, n_new, a, b, L);
       }
+      FJG_PH(if (r0 == 0) ph_resc += clock64() - ph1;)
     }
     __syncthreads();  // B2: new jet and compaction written, rescan partials ready
+    FJG_PH(const long long ph2 = clock64(); ph_s2 += ph2 - ph1;)
     n = n_new;
     ++step;
     if (n == 0) break;
@@ -778,6 +829,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       __syncwarp();
     }
     __syncthreads();  // B3: the new jet's partials are ready
+    FJG_PH(ph_b3 = clock64(); ph_s3 += ph_b3 - ph2;)
     if (pair && warp == (a % T) / 32) {
       Cert x = (lane < W) ? S.wcert[lane] : cert_empty();
       x = cert_warp(x);
@@ -798,6 +850,18 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
   // parents (owner[label] = parent label, or -(jet+1) once promoted)
   __syncthreads();
   if (tid == 0) A.n_jets[e] = S.ctl_njets;
+  FJG_PH(if (A.phase) {
+    if (tid == 0) {
+      atomicAdd(A.phase + kPhS1, (unsigned long long)ph_s1);
+      atomicAdd(A.phase + kPhS2, (unsigned long long)ph_s2);
+      atomicAdd(A.phase + kPhS3, (unsigned long long)ph_s3);
+      atomicAdd(A.phase + kPhTail, (unsigned long long)ph_tail);
+      atomicAdd(A.phase + kPhSteps, (unsigned long long)step);
+      atomicAdd(A.phase + kPhEvents, 1ull);
+    }
+    if (warp < MW && lane == 0) atomicAdd(A.phase + kPhKin0 + warp, (unsigned long long)ph_kin);
+    if (tid == 32 * MW) atomicAdd(A.phase + kPhRescan, (unsigned long long)ph_resc);
+  })
   if (A.owner) {
     for (int s = tid; s < N; s += T) {
       int x = s, guard = 0;

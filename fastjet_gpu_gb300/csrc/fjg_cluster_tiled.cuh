@@ -31,13 +31,32 @@
 //
 // Tile lists.  Per tile, a list of member slots with S.slack free entries
 // after the live ones.  Removal writes a tombstone (-1) in place; a new jet
-// that changes tile is appended.  A reader running concurrently with these
-// updates sees either the old or the new word of any entry, and every reader
-// skips the slots involved in the merge by name, so no reader needs the
-// update to be finished.  The lists are rebuilt (tombstones squeezed out,
-// slack restored) every S.slack steps; at most one entry is appended per
-// step.  The slack is what the list area spares per tile (kListSlack entries
-// per possible tile, spread over the tiles in use), at most kTileSlackMax.
+// that changes tile is appended.  The lists are rebuilt (tombstones squeezed
+// out, every slack entry set to -1) every S.slack steps; at most one entry is
+// appended per step.  The slack is what the list area spares per tile
+// (kListSlack entries per possible tile, spread over the tiles in use), at
+// most kTileSlackMax.
+//
+// The update runs on thread 0 in S3a while the other warps scan windows for
+// the step's targets, with no barrier or fence between them.  Its stores, and
+// what a concurrent reader of the same words can observe (32-bit words, so
+// each load returns the old or the new value, never a mix):
+//   (1) members[start[tile b] + pos b] = -1: the reader sees b or -1;
+//   (2) when a changes tile, members[start[old tile a] + pos a] = -1: a or -1;
+//   (3) members[start[ta] + p] = a with p = count[ta], then count[ta] = p + 1:
+//       a reader holding the old count never reaches entry p; one holding the
+//       new count reads entry p as a or as its previous word, and that word
+//       is -1 -- entry p lies past every count this tile has had since the
+//       last rebuild (counts only grow between rebuilds, by one per append),
+//       so nothing has written it since the rebuild set it to -1;
+//   (4) pos[a], tile[a], alive[b] and the referrer counts of a and of one
+//       dropped neighbour: no S3a reader uses them for a, b or as an index.
+// Every outcome is a, b or -1, and every reader skips -1 and the merged slots
+// c and j by name ({a, b} = {c, j}); the new jet a enters the targets'
+// searches explicitly (`extra`), not through the lists.  So the scans find
+// the same candidates whichever words they see.  Lengths are read once and
+// clamped to the list capacity, which the slack bounds as above.  The
+// barrier B3 then orders the completed update before the next readers.
 //
 // Per step (T = 256 threads, 8 warps):
 //   S1  argmin over the tile summaries (smallest klo, its slot and khi,
@@ -759,7 +778,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       }
     }
     if (c < 0) {
-      if (tid == 0) atomicOr(A.status, 4);
+      if (tid == 0) raise_event_status(A, e, kStatusInternal);
       break;
     }
 

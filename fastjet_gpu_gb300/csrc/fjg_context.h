@@ -84,6 +84,7 @@ struct fjg_ctx {
   fjg::Tuning tune = fjg::default_tuning();
   double tuned_rate[fjg::kNumBuckets] = {};
   std::string last_error;
+  unsigned long long* phase = nullptr;  // [kPhSlots] phase counters (FJG_PHASE_CLOCKS builds only)
 };
 
 namespace fjg {

@@ -26,7 +26,7 @@ fjg_status fjg_graph_capture_batch(fjg_ctx* ctx, const double* p4, const int64_t
     return set_error(ctx, FJG_EINVAL, "bad batch arguments");
   if (total > 0 && (!p4 || !out->jets || !out->jet_label)) return set_error(ctx, FJG_EINVAL, "null buffer");
   if (!algo && !fjg::valid_algo(algo_all)) return set_error(ctx, FJG_EINVAL, "bad algorithm");
-  if (!radius && !(r_all > 0.0)) return set_error(ctx, FJG_EINVAL, "R must be positive");
+  if (!radius && !fjg::valid_radius(r_all)) return set_error(ctx, FJG_EINVAL, "R must be finite and >= 0");
   DeviceGuard dg(ctx->device);
   fjg_graph* g = new (std::nothrow) fjg_graph();
   if (!g) return set_error(ctx, FJG_ENOMEM, "host allocation failed");

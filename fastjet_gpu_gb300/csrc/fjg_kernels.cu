@@ -16,6 +16,7 @@ __global__ void __launch_bounds__(kTiledT, 1) k_cluster_tiled(BatchArgs A) {
     __syncthreads();
     const int e = S.event;
     if (e < 0) break;
+    if (refused_event(A, e)) continue;  // ends with a barrier
     cluster_event_tiled(S, A, A.large_ws, e);  // ends with a barrier
     if (threadIdx.x == 0) signal_done(A, e);
   }
@@ -69,16 +70,22 @@ cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
 // Events above kSmemMaxN particles go straight to the large list (or raise
 // kStatusTooBig when there is no large workspace, or it is too small).
 // Input check, one warp per event: n_jets[e] = -1 when a momentum component
-// is not finite (the event is then refused: kStatusBadArg), else 0.  Events
-// of no or too many particles are left to the bucketing.
+// is not finite, when the event's particle range does not lie inside
+// [0, ws_particles) -- the workspace the kernels index by the same offsets --,
+// or when its algorithm code (per-event array) is not kt, C/A or anti-kt or
+// its R (per-event array) is not finite and >= 0 (the event is then refused:
+// kStatusBadArg), else 0.  Events of no or too many particles are left to the
+// bucketing.
 __global__ void k_check_events(const double* p4, int p4_stride, const int64_t* offsets, int n_events,
-                               int32_t* n_jets) {
+                               int32_t* n_jets, int64_t ws_particles, const int32_t* algo, const double* radius) {
   const int lane = threadIdx.x & 31;
   const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int e = w0; e < n_events; e += nw) {
     const int64_t o0 = offsets[e], o1 = offsets[e + 1];
-    bool bad = false;
-    if (o1 - o0 > 0 && o1 - o0 <= kLargeMaxN) {
+    bool bad = o1 > o0 && (o0 < 0 || o1 > ws_particles);
+    if (algo) bad |= algo[e] < -1 || algo[e] > 1;
+    if (radius) bad |= !(radius[e] >= 0.0 && isfinite(radius[e]));
+    if (!bad && o1 - o0 > 0 && o1 - o0 <= kLargeMaxN) {
       for (int64_t s = o0 + lane; s < o1; s += 32) {
         const double* p = p4 + s * p4_stride;
         bad |= !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) && isfinite(p[3]));
@@ -87,6 +94,31 @@ __global__ void k_check_events(const double* p4, int p4_stride, const int64_t* o
     bad = __any_sync(0xffffffffu, bad);
     if (lane == 0) n_jets[e] = bad ? -1 : 0;
   }
+}
+
+// Input check of a request server's micro-batch ((start, end) pairs), one
+// warp per event: an event with a non-finite momentum component gets
+// kStatusBadArg in its own status word, so the clustering kernel skips it and
+// only its request fails.
+__global__ void k_check_pairs(const double* p4, const int64_t* pairs, int n_events, int32_t* ev_status) {
+  const int lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int e = w0; e < n_events; e += nw) {
+    const int64_t o0 = pairs[2 * (int64_t)e], o1 = pairs[2 * (int64_t)e + 1];
+    bool bad = false;
+    for (int64_t s = o0 + lane; s < o1; s += 32) {
+      const double* p = p4 + 4 * s;
+      bad |= !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) && isfinite(p[3]));
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) ev_status[e] |= kStatusBadArg;
+  }
+}
+
+cudaError_t launch_check_pairs(const double* p4, const int64_t* pairs, int n_events, int32_t* ev_status,
+                               cudaStream_t s) {
+  const int grid = (n_events + 7) / 8 > 1024 ? 1024 : (n_events + 7) / 8;  // 8 events (warps) per block
+  k_check_pairs<<<grid < 1 ? 1 : grid, 256, 0, s>>>(p4, pairs, n_events, ev_status);
+  return cudaGetLastError();
 }
 
 __global__ void k_size_hist(const int64_t* offsets, int n_events, int32_t* hist, int32_t* n_jets, int* status,
@@ -216,7 +248,8 @@ static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_e
   if ((err = cudaMemsetAsync(sc.counts + kLargeQueue, 0, sizeof(int32_t), stream)) != cudaSuccess) return err;
   const int grid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
   const int cgrid = n_events / 8 + 1 > 2048 ? 2048 : n_events / 8 + 1;  // 8 events (warps) per block
-  k_check_events<<<cgrid, 256, 0, stream>>>(base.p4, base.p4_stride, base.offsets, n_events, base.n_jets);
+  k_check_events<<<cgrid, 256, 0, stream>>>(base.p4, base.p4_stride, base.offsets, n_events, base.n_jets,
+                                            sc.ws_stride, base.algo, base.radius);
   int32_t* large_order = sc.order + kLargeQueue * sc.cap_events;
   k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status, large_order,
                                         sc.counts + kLargeQueue, sc.large_ws ? sc.large_ws_particles : 0);

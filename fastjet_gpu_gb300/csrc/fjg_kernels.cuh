@@ -24,8 +24,12 @@ __host__ __device__ inline int bucket_of(int n) {
   return n <= 256 ? 0 : n <= 512 ? 1 : n <= 1024 ? 2 : n <= 2048 ? 3 : n <= 4096 ? 4 : -1;
 }
 
-// Status bits raised by kernels (ORed into the device status word).
-enum : int { kStatusTooBig = 1, kStatusBadArg = 2, kStatusInternal = 4 };
+// R accepted by the entry points: finite and >= 0.  R = 0 is allowed, as the
+// reference driver allows it (main.cc:159): 1/R^2 is then infinite, every pair
+// distance is infinite (NaN for coincident pseudojets, which never undercuts a
+// beam distance either), so every particle is promoted to a jet in order of
+// its weight -- what the reference's cluster() computes (tri_matrix.cu:305).
+inline bool valid_radius(double r) { return r >= 0.0 && r <= 1.7976931348623157e308; }
 
 // Compiled variants of the shared-memory kernel: CTA size and slots per
 // thread (capacity = their product).  A bucket of capacity 256 << b can run
@@ -138,6 +142,11 @@ cudaError_t launch_batch_on_stream(const BatchArgs& base, const Scratch& sc, int
 // One event, one CTA (the plain per-event-launch path; the tiled kernel above
 // kSmemMaxN particles).
 cudaError_t launch_single(const BatchArgs& base, const Scratch& sc, int n, const Tuning& tune, cudaStream_t stream);
+
+// Finiteness check of a request server's micro-batch ((start, end) pairs of
+// [n][4] momenta): bad events get kStatusBadArg in ev_status.
+cudaError_t launch_check_pairs(const double* p4, const int64_t* pairs, int n_events, int32_t* ev_status,
+                               cudaStream_t s);
 
 // Scatter jets into the reference's PseudoJet records (in place).
 cudaError_t launch_pseudojet_epilogue(void* records, int size, const double* jets, const int32_t* jet_label,

@@ -14,16 +14,25 @@
 // which loads this library holds until the process exits.  The host cannot use
 // the array's name as a device address, so the first call on each device
 // looks the address up with cudaGetSymbolAddress (with that device current)
-// and caches it; that first call should therefore come before any stream
-// capture.  All calls share the array: each call clears the counters and the
-// error word before its kernels run, and calls whose work overlaps on the GPU
-// (different streams or host threads without ordering) race on it.
+// and caches it.  Every call reads the kernels' status word back and
+// synchronises its stream, so no call can be made inside stream capture.
+// All calls share the array: each call clears the counters and the error word
+// before its kernels run, and calls whose work overlaps on the GPU (different
+// streams or host threads without ordering) race on it.
+//
+// Bounds: the input check refuses events whose range [offsets[e],
+// offsets[e+1]) leaves [0, kNoAllocMaxParticles), the extent of the
+// per-particle workspace.  An event above 4096 particles uses
+// large_ws_bytes(N) <= 91 N + 31 < kLargeWsBytesPerParticle * N bytes from
+// kLargeWsBytesPerParticle * offsets[e] on, so its region ends inside the
+// large workspace too (no margin is needed past the last particle).
 #include <cstdint>
 #include <mutex>
 
 #include <cuda_runtime.h>
 
 #include "fastjet_gb300.h"
+#include "fjg_context.h"
 #include "fjg_kernels.cuh"
 
 namespace {
@@ -69,7 +78,7 @@ extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t*
     return fail(FJG_EINVAL, "fjg_cluster_batch_noalloc: more particles than FJG_NOALLOC_MAX_PARTICLES in one call");
   if (!algo && !(algo_all == FJG_KT || algo_all == FJG_CAM || algo_all == FJG_ANTIKT))
     return fail(FJG_EINVAL, "bad algorithm");
-  if (!radius && !(r_all > 0.0)) return fail(FJG_EINVAL, "R must be positive");
+  if (!radius && !fjg::valid_radius(r_all)) return fail(FJG_EINVAL, "R must be finite and >= 0");
 
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(FJG_ECUDA, "no usable CUDA device");
@@ -129,8 +138,6 @@ extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t*
   if (err == cudaSuccess) err = cudaMemcpyAsync(&st, sc.status, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);
   if (err != cudaSuccess) return fail(err == cudaErrorMemoryAllocation ? FJG_ENOMEM : FJG_ECUDA, cudaGetErrorString(err));
-  if (st & fjg::kStatusTooBig) return fail(FJG_ETOOBIG, "an event exceeds the supported particle count");
-  if (st & fjg::kStatusInternal) return fail(FJG_EKERNEL, "a clustering kernel found no candidate");
-  if (st) return fail(FJG_EINVAL, "invalid event offsets");
-  return FJG_OK;
+  // the same status words and messages as the context entry points
+  return fjg::status_to_error(nullptr, st);
 }

@@ -69,6 +69,7 @@ struct Block {
   double* radius;      // [max_batch]
   int32_t* done_slot;  // [max_batch]
   int32_t* n_jets;     // [max_batch]
+  int32_t* ev_status;  // [max_batch] per-event status bits (0: fine)
   int32_t* count;      // [1]
 };
 
@@ -82,6 +83,7 @@ struct Lane {
   int* d_queue = nullptr;   // work-queue head (device)
   int* d_status = nullptr;  // kernel status word (device)
   int* h_status = nullptr;  // its copy (pinned), valid once ev completes
+  int attributed = 0;       // status bits of the micro-batch's requests seen so far
 };
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
@@ -157,6 +159,14 @@ void arena_free(fjg_server* S, int64_t start, int64_t n) {
   S->free_ranges.emplace(start, n);
 }
 
+// A request's result status from its per-event status bits.
+int event_status(int bits) {
+  if (!bits) return FJG_OK;
+  if (bits & fjg::kStatusTooBig) return FJG_ETOOBIG;
+  if (bits & fjg::kStatusInternal) return FJG_EKERNEL;
+  return FJG_EINVAL;
+}
+
 void finish(fjg_server* S, Req* r, int status) {
   r->status = status;
   r->state = kDone;
@@ -175,6 +185,7 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
     L.host.radius[i] = r->r;
     L.host.done_slot[i] = r->slot;
     L.host.n_jets[i] = 0;
+    L.host.ev_status[i] = 0;
     r->state = kRunning;
     L.batch.push_back(r);
   }
@@ -202,8 +213,16 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
   A.serve_order = 1;  // small events first: they are the latency-bound requests
   A.done = S->d_done;
   A.done_slot = L.dev.done_slot;
+  A.ev_status = L.dev.ev_status;
+  L.attributed = 0;
   cudaError_t err = cudaMemsetAsync(L.d_queue, 0, 2 * sizeof(int), L.stream);  // queue head and status
   if (err != cudaSuccess) return err;
+  if (S->cfg.flags & FJG_SERVE_DEVICE_CHECK) {
+    // momenta checked on the device: a request with a non-finite component
+    // gets its own status word set and is skipped by the clustering kernel
+    err = fjg::launch_check_pairs(S->d_p4, L.dev.offsets, m, L.dev.ev_status, L.stream);
+    if (err != cudaSuccess) return err;
+  }
   if (q == fjg::kLargeQueue) {
     const int grid = std::min(m, ctx->num_sms * ctx->tune.large_ctas_per_sm);
     err = fjg::launch_tiled(A, grid, L.stream);
@@ -235,8 +254,10 @@ bool progress(fjg_server* S) {
       if (!r) continue;  // completed earlier (and possibly returned and released since)
       if (__atomic_load_n(&S->h_done[r->slot], __ATOMIC_ACQUIRE)) {
         r->n_jets = __atomic_load_n(&L.host.n_jets[i], __ATOMIC_ACQUIRE);
+        const int bits = __atomic_load_n(&L.host.ev_status[i], __ATOMIC_ACQUIRE);
+        L.attributed |= bits;
         S->inflight[r->bucket]--;
-        finish(S, r, FJG_OK);
+        finish(S, r, event_status(bits));  // a failed request fails alone
         L.batch[i] = nullptr;
       } else if (ended) {
         S->inflight[r->bucket]--;
@@ -245,9 +266,10 @@ bool progress(fjg_server* S) {
       }
     }
     if (!ended) continue;
-    // inputs are checked to be finite at submission, so a kernel status
-    // word other than 0 means the server can no longer be trusted
-    if (st != 0) S->failed = true;
+    // every status bit a clustering kernel raises is also recorded in the
+    // event's own word and failed that request alone; a bit that no request
+    // accounts for means the server can no longer be trusted
+    if (st & ~L.attributed) S->failed = true;
     L.busy = false;
     L.batch.clear();
   }
@@ -316,11 +338,12 @@ fjg_status submit_req(fjg_server* S, Req* r) {
 fjg_status check_event(fjg_server* S, const double* p4, int n, int algo, double r) {
   if (n < 0 || (n > 0 && !p4)) return set_error(S->ctx, FJG_EINVAL, "bad event");
   if (!fjg::valid_algo(algo)) return set_error(S->ctx, FJG_EINVAL, "bad algorithm");
-  if (!(r > 0.0)) return set_error(S->ctx, FJG_EINVAL, "R must be positive");
+  if (!fjg::valid_radius(r)) return set_error(S->ctx, FJG_EINVAL, "R must be finite and >= 0");
   if (n > S->cfg.arena_particles || n > fjg::kLargeMaxN)
     return set_error(S->ctx, FJG_ETOOBIG, "event larger than the server's arena");
-  for (int64_t i = 0; i < 4 * (int64_t)n; ++i)
-    if (!std::isfinite(p4[i])) return set_error(S->ctx, FJG_EINVAL, "non-finite momentum");
+  if (!(S->cfg.flags & FJG_SERVE_DEVICE_CHECK))
+    for (int64_t i = 0; i < 4 * (int64_t)n; ++i)
+      if (!std::isfinite(p4[i])) return set_error(S->ctx, FJG_EINVAL, "non-finite momentum");
   return FJG_OK;
 }
 
@@ -351,7 +374,8 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
   const size_t b_hist = hist ? al(sizeof(fjg_step) * (size_t)P) : 0, b_own = hist ? al(4 * (size_t)P) : 0;
   const size_t b_done = al(4 * (size_t)c.max_inflight);
   const size_t per_block = al(16 * (size_t)c.max_batch) + al(4 * (size_t)c.max_batch) + al(8 * (size_t)c.max_batch) +
-                           al(4 * (size_t)c.max_batch) + al(4 * (size_t)c.max_batch) + 256;
+                           al(4 * (size_t)c.max_batch) + al(4 * (size_t)c.max_batch) + al(4 * (size_t)c.max_batch) +
+                           256;
   cudaError_t err = cudaHostAlloc(&S->host_mem, b_p4 + b_jets + b_lab + b_hist + b_own + b_done,
                                   cudaHostAllocMapped | cudaHostAllocPortable);
   if (err == cudaSuccess)
@@ -407,12 +431,15 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
       p += al(4 * (size_t)c.max_batch);
       L.host.n_jets = reinterpret_cast<int32_t*>(p);
       p += al(4 * (size_t)c.max_batch);
+      L.host.ev_status = reinterpret_cast<int32_t*>(p);
+      p += al(4 * (size_t)c.max_batch);
       L.host.count = reinterpret_cast<int32_t*>(p);
       L.dev.offsets = static_cast<int64_t*>(dev_of(L.host.offsets));
       L.dev.algo = static_cast<int32_t*>(dev_of(L.host.algo));
       L.dev.radius = static_cast<double*>(dev_of(L.host.radius));
       L.dev.done_slot = static_cast<int32_t*>(dev_of(L.host.done_slot));
       L.dev.n_jets = static_cast<int32_t*>(dev_of(L.host.n_jets));
+      L.dev.ev_status = static_cast<int32_t*>(dev_of(L.host.ev_status));
       L.dev.count = static_cast<int32_t*>(dev_of(L.host.count));
       L.d_queue = S->d_words + 2 * k;
       L.d_status = S->d_words + 2 * k + 1;

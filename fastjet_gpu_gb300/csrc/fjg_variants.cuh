@@ -27,6 +27,7 @@ __device__ __forceinline__ void smem_event_loop(const BatchArgs& A) {
     __syncthreads();
     const int e = S.event;
     if (e < 0) break;
+    if (refused_event(A, e)) continue;  // ends with a barrier
     cluster_event_smem<T, SPT>(S, A, e);  // ends with a barrier
     if (threadIdx.x == 0) signal_done(A, e);
   }

@@ -96,6 +96,16 @@ const char* fjg_status_string(fjg_status s);
 fjg_status fjg_ctx_check(fjg_ctx* ctx);
 /* Last error message of the context (or of the calling thread when ctx is NULL). */
 const char* fjg_last_error(const fjg_ctx* ctx);
+/* Per-step phase counters of the shared-memory clustering kernel, summed over
+ * the events clustered through this context's batch and one-event calls:
+ * out[0..3] clock cycles in the argmin, merge, new-jet and neighbour-resolution
+ * phases as the CTA's thread 0 sees them, out[4..6] in the merge warps'
+ * kinematics chains, out[7] in the first rescan thread's merge-phase work,
+ * out[8] steps, out[9] events (n <= 16 entries).  Only a library built with
+ * -DFJG_PHASE_CLOCKS (python -m fastjet_gpu_gb300.build --phase-clocks) has
+ * them; the product build returns FJG_EINVAL.  Waits for the context stream;
+ * `reset` zeroes them.  No counterpart in the reference. */
+fjg_status fjg_phase_clocks(fjg_ctx* ctx, unsigned long long* out, int n, int reset);
 
 /* Batched clustering of device-resident events (the persistent-kernel path).
  *   p4      device [total][4] FP64 px, py, pz, E
@@ -262,15 +272,24 @@ typedef struct {
   int32_t streams;         /* micro-batch streams; default 16 */
   int32_t max_batch;       /* events per micro-batch; default 512 */
   int32_t oversubscribe;   /* launched events per resident CTA slot of a bucket; default 2 */
-  int32_t flags;           /* FJG_SERVE_HISTORY: also return the merge history and constituents */
+  int32_t flags;           /* FJG_SERVE_HISTORY, FJG_SERVE_DEVICE_CHECK (below) */
 } fjg_server_config;
+/* Also return the merge history and constituents of every request. */
 #define FJG_SERVE_HISTORY 1
+/* Check momenta for NaN/inf on the GPU, as a micro-batch is launched, instead
+ * of on the host at submission (which costs a pass over the request on the
+ * submitting thread).  A request that fails the check completes with status
+ * FJG_EINVAL and no jets; the other requests of its micro-batch are clustered
+ * as usual. */
+#define FJG_SERVE_DEVICE_CHECK 2
 
 /* One completed request.  The pointers are into the server's arena and stay
  * valid until fjg_server_release(ticket). */
 typedef struct {
   uint64_t ticket;
-  int32_t status;          /* FJG_OK or the kernel's error */
+  int32_t status;          /* FJG_OK, or this request's own error (FJG_EINVAL: refused input;
+                              FJG_EKERNEL: a kernel inconsistency); a failed request does
+                              not affect the others */
   int32_t n_particles;
   int32_t n_jets;
   const double* jets;      /* [n_jets][4], in promotion order */
@@ -318,9 +337,13 @@ fjg_status fjg_server_replay(fjg_server* server, const double* p4, const int64_t
  * FJG_EINVAL).  The
  * kernels' bookkeeping and per-particle working state live in a static device
  * array of FJG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds
- * until exit.  The first call on each device looks up that array's address; make it
- * before any stream capture.  Calls share the array: calls whose work overlaps
- * on the GPU race and must be serialised by the caller. */
+ * until exit.  The first call on each device also looks up that array's
+ * address.  Every call synchronises `stream` before it returns (it reads the
+ * kernels' status word back), so the entry point cannot be used inside stream
+ * capture.  Calls share the array: calls whose work overlaps on the GPU race
+ * and must be serialised by the caller.  Event ranges outside
+ * [0, FJG_NOALLOC_MAX_PARTICLES) are refused (FJG_EINVAL), as are
+ * non-finite momenta. */
 #define FJG_NOALLOC_MAX_EVENTS 65536
 #define FJG_NOALLOC_MAX_PARTICLES 131072
 #define FJG_NOALLOC_SCRATCH_BYTES ((7 * 8 + 96) * FJG_NOALLOC_MAX_PARTICLES + 6 * 4 * FJG_NOALLOC_MAX_EVENTS + 32768)

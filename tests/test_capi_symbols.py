@@ -80,3 +80,25 @@ def test_host_side_argument_checks():
         st = L.fjg_ctx_create(0, ctypes.byref(h))
         assert st != 0 and not h.value
         assert L.fjg_last_error(None)
+
+
+def test_noalloc_limits_refused_before_device_work():
+    """fjg_cluster_batch_noalloc refuses batches beyond its static scratch
+    (more than FJG_NOALLOC_MAX_EVENTS events or FJG_NOALLOC_MAX_PARTICLES
+    particles) with FJG_EINVAL before touching a device."""
+    import fastjet_gpu_gb300 as F
+    text = open(os.path.join(ROOT, "include", "fastjet_gb300.h")).read()
+    max_events = int(re.search(r"#define FJG_NOALLOC_MAX_EVENTS (\d+)", text).group(1))
+    max_particles = int(re.search(r"#define FJG_NOALLOC_MAX_PARTICLES (\d+)", text).group(1))
+    L = F.lib()
+    f = L.fjg_cluster_batch_noalloc
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int,
+                  ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(F._Outputs), ctypes.c_void_p]
+    dummy = ctypes.c_void_p(64)  # never dereferenced: the calls are refused first
+    out = F._Outputs(dummy.value, dummy.value, dummy.value, None, None)
+    st = f(dummy, dummy, 1, max_particles + 1, None, -1, None, 0.4, ctypes.byref(out), None)
+    assert st == 1 and b"FJG_NOALLOC_MAX_PARTICLES" in L.fjg_last_error(None)
+    st = f(dummy, dummy, max_events + 1, 10, None, -1, None, 0.4, ctypes.byref(out), None)
+    assert st == 1 and b"FJG_NOALLOC_MAX_EVENTS" in L.fjg_last_error(None)
+    st = f(dummy, dummy, 1, 10, None, 5, None, 0.4, ctypes.byref(out), None)
+    assert st == 1 and b"algorithm" in L.fjg_last_error(None)

@@ -26,13 +26,15 @@ def _batch(evs):
 
 
 def test_reference_goldens_bit_exact(ctx):
-    """Every reference golden case (552): identical jet sets, bit for bit."""
+    """Every reference golden case (552, plus 8 of pile-up-like events of
+    10k-22k particles from the reference's grid backend): identical jet sets,
+    bit for bit."""
     by = collections.defaultdict(list)
     for case in G.cases():
         by[(case[0], case[1], case[2])].append(case)
     n = 0
     for (name, algo, radius), cs in sorted(by.items()):
-        evs = G.inputs(name)
+        evs = G.golden_events(name)
         p4, off = _batch(evs)
         res = ctx.cluster_batch(p4, off, G.ALGO_CODE[algo], float(radius))
         for _, _, _, ev, nj, dg in cs:
@@ -41,7 +43,39 @@ def test_reference_goldens_bit_exact(ctx):
             jets = res["jets"][off[ev]:off[ev] + got]
             assert G.jets_digest(jets) == dg, (name, algo, radius, ev)
             n += 1
-    assert n == 552
+    assert n == 552 + 8
+
+
+def test_reference_merge_histories(ctx):
+    """The GPU's merge sequence is the reference's own (tri_matrix and grid,
+    recorded by their step printfs; tests/golden/ref_history.json), step by
+    step up to the order inside ties and near ties (golden_util.
+    near_tie_mismatch), for every recorded case: the fixtures, the synthetic
+    events and the 10k-22k-particle events; and the distances agree within
+    the kinematics tolerance."""
+    import oracle
+    cases = G.history_cases()
+    groups = collections.defaultdict(list)
+    for key in cases:
+        name, backend, algo, radius = key.split(".", 3)
+        groups[(name, algo, radius)].append(key)
+    checked = 0
+    for (name, algo, radius), keys in sorted(groups.items()):
+        evs = G.golden_events(name)
+        p4, off = _batch(evs)
+        res = ctx.cluster_batch(p4, off, G.ALGO_CODE[algo], float(radius), history=True)
+        h = res["history"]
+        ohist = oracle.cluster_batch(p4, off, G.ALGO_CODE[algo], float(radius), threads=16, portable=True)[0]
+        for key in keys:
+            ra, rb, rd = G.reference_history(key, ohist)
+            for e in range(len(evs)):
+                s0, s1 = off[e], off[e + 1]
+                k, _ = G.near_tie_mismatch(h["a"][s0:s1], h["b"][s0:s1], h["d"][s0:s1], ra[s0:s1], rb[s0:s1],
+                                           rd[s0:s1])
+                assert k < 0, f"{key} event {e}: GPU merge sequence differs from the reference at step {k}"
+            np.testing.assert_allclose(h["d"], rd, rtol=U.D_RTOL, atol=0, err_msg=key)
+            checked += 1
+    assert checked == len(cases)
 
 
 @pytest.mark.parametrize("algo", [1, 0, -1])
@@ -231,4 +265,53 @@ def test_non_finite_momenta_are_refused(ctx):
     one = torch.from_numpy(bad_p[b.offsets[3]:b.offsets[4]].copy()).cuda()
     with pytest.raises(F.FjgError):
         ctx.cluster_event(one, -1, 0.4)
+    ctx.cluster_batch(b.particles, b.offsets, -1, 0.4)  # the context stays usable
+
+
+def test_zero_radius(ctx):
+    """R = 0, which the reference driver accepts (main.cc:159): 1/R^2 is
+    infinite, so every particle is promoted, in order of weight, by the batch,
+    one-event and PseudoJet paths, small and tiled kernels alike."""
+    import torch
+    evs = [E.single_event(n, 2, seed=90 + n) for n in (1, 2, 37, 700)] + [E.portable_event(5000, 3, seed=91)]
+    p4, off = _batch(evs)
+    for algo in (1, 0, -1):
+        res = ctx.cluster_batch(p4, off, algo, 0.0, history=True, owner=True)
+        for e, ev in enumerate(evs):
+            o0, o1 = off[e], off[e + 1]
+            assert res["n_jets"][e] == ev.shape[0]
+            assert np.all(res["history"][o0:o1]["b"] == -1)
+            U.compare_event(ev, algo, 0.0, res["jets"][o0:o1], res["n_jets"][e], res["history"][o0:o1],
+                            res["owner"][o0:o1], ctx=f"R=0 n={ev.shape[0]} algo={algo}")
+    one = ctx.cluster_event(torch.from_numpy(evs[3]).cuda(), -1, 0.0, history=True)
+    assert int(one["n_jets"][0]) == evs[3].shape[0]
+
+
+def test_bad_per_event_arguments_are_refused(ctx):
+    """Per-event algorithm codes outside {kt, C/A, anti-kt} and radii that are
+    negative or not finite are refused on the device (no jets, FJG_EINVAL);
+    the other events are clustered as usual; scalar ones on the host."""
+    import fastjet_gpu_gb300 as F
+    b = E.mixed_batch(8, 20, 600, seed=62)
+    algo = np.full(b.n_events, -1, np.int32)
+    radius = np.full(b.n_events, 0.4)
+    clean = ctx.cluster_batch(b.particles, b.offsets, algo, radius)
+    algo[1] = 5
+    radius[4] = -0.4
+    radius[6] = np.nan
+    with pytest.raises(F.FjgError):
+        ctx.cluster_batch(b.particles, b.offsets, algo, radius)
+    import torch
+    out = ctx.cluster_batch_device(torch.from_numpy(b.particles).cuda(), torch.from_numpy(b.offsets).cuda(),
+                                   torch.from_numpy(algo).cuda(), torch.from_numpy(radius).cuda())
+    torch.cuda.synchronize()
+    with pytest.raises(F.FjgError):
+        ctx.check()
+    nj = out["n_jets"].cpu().numpy()
+    assert nj[1] == 0 and nj[4] == 0 and nj[6] == 0
+    for e in (0, 2, 3, 5, 7):
+        assert nj[e] == clean["n_jets"][e]
+    for bad_r in (-1.0, float("nan"), float("inf")):
+        with pytest.raises(F.FjgError):
+            ctx.cluster_batch(b.particles, b.offsets, -1, bad_r)
     ctx.cluster_batch(b.particles, b.offsets, -1, 0.4)  # the context stays usable

@@ -98,7 +98,7 @@ def test_server_rejects_bad_requests(ctx):
         assert ei.value.status == 4
         bad = ev.copy()
         bad[3, 2] = np.nan
-        for args in ((bad, -1, 0.4), (ev, 2, 0.4), (ev, -1, 0.0)):
+        for args in ((bad, -1, 0.4), (ev, 2, 0.4), (ev, -1, -0.4), (ev, -1, float("nan"))):
             with pytest.raises(F.FjgError) as ei:
                 srv.submit(*args)
             assert ei.value.status == 1
@@ -127,3 +127,31 @@ def test_server_replay_open_loop(ctx):
         srv.close()
     assert lat.shape == (batch.n_events,) and np.all(lat > 0)
     assert wall >= arrival[-1]
+
+
+def test_server_poisoned_request_fails_alone(ctx):
+    """With the momenta checked on the GPU (device_check), a request with a
+    NaN or infinite component reaches the kernels: it completes with FJG_EINVAL
+    and no jets, while the requests launched in the same micro-batches -- small
+    and tiled alike -- complete as if it were not there, and the server keeps
+    serving.  The fault is injected on the host (bad input); nothing faults."""
+    import fastjet_gpu_gb300 as F
+    batch, algo, radius = E.serving_mix(40, seed=14, hi=7000)
+    events = [batch.event(e).copy() for e in range(batch.n_events)]
+    sizes = np.array([ev.shape[0] for ev in events])
+    small = int(np.flatnonzero(sizes <= 2048)[0])
+    large = int(np.flatnonzero(sizes > 4096)[0])
+    events[small][1, 0] = np.nan
+    events[large][-1, 3] = np.inf
+    srv = F.Server(ctx, history=True, device_check=True, max_batch=64)
+    try:
+        res = _drive(srv, events, algo, radius, per_poll=40, seed=4)
+        again = _drive(srv, [batch.event(0)], algo[:1], radius[:1])
+    finally:
+        srv.close()
+    for e, ev in enumerate(events):
+        if e in (small, large):
+            assert res[e]["status"] == 1 and res[e]["n_jets"] == 0, e
+            continue
+        _same(ctx, res[e], ev, int(algo[e]), float(radius[e]), f"event {e}")
+    _same(ctx, again[0], batch.event(0), int(algo[0]), float(radius[0]), "after the poisoned requests")
