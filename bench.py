@@ -637,7 +637,7 @@ def run_ours(args, rank, world, local_rank):
                              {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                               "frac": achieved / peak,
                               "note": f"whole step, staging only ({alg_bytes} B per step); peak {peak_kind}"}]},
-            "gpu_launches": args.steps * 11,  # input check, 4 bucketing kernels, the tiled kernel, 5 bucket kernels
+            "gpu_launches": args.steps * 12,  # 2 input checks, 4 bucketing kernels, the tiled kernel, 5 buckets
             "clocks": clk.summary(),
             "wall_s": t_wall}
     if second is not None:

@@ -231,15 +231,17 @@ class Context:
         self._check(lib().fjg_ctx_check(self._h))
 
     PHASES = ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
-              "rescan_s2", "steps", "events")
+              "rescan_s2", "steps", "events", None, None,
+              "t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3a_lists_targets", "t_s3b_window",
+              "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2", "t_steps", "t_events")
 
     def phase_clocks(self, reset=False):
-        """Per-step phase counters of the shared-memory kernel (only in the
+        """Per-step phase counters of the clustering kernels (only in the
         -DFJG_PHASE_CLOCKS build, see fastjet_gpu_gb300.phases): a dict of
-        summed clock cycles per phase, steps and events."""
-        buf = (ctypes.c_ulonglong * 16)()
-        self._check(lib().fjg_phase_clocks(self._h, buf, 16, 1 if reset else 0))
-        return {k: int(buf[i]) for i, k in enumerate(self.PHASES)}
+        summed clock cycles per phase, steps and events (t_*: tiled kernel)."""
+        buf = (ctypes.c_ulonglong * 24)()
+        self._check(lib().fjg_phase_clocks(self._h, buf, 24, 1 if reset else 0))
+        return {k: int(buf[i]) for i, k in enumerate(self.PHASES) if k}
 
     def _after_torch(self, device):
         """Make the context's stream wait for torch's current stream."""

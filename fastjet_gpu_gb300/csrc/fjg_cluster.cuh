@@ -51,7 +51,13 @@ namespace fjg {
 // warp the length of its kinematics chain, and the first rescan thread the
 // time of its S2 work.  At the end of an event they are added to A.phase.
 enum PhaseSlot {
-  kPhS1 = 0, kPhS2, kPhS3, kPhTail, kPhKin0, kPhKin1, kPhKin2, kPhRescan, kPhSteps, kPhEvents, kPhSlots = 16
+  kPhS1 = 0, kPhS2, kPhS3, kPhTail, kPhKin0, kPhKin1, kPhKin2, kPhRescan, kPhSteps, kPhEvents,
+  // the tiled kernel (events above 4096 particles): rebuild of the tile lists,
+  // argmin, merge || target detection, lists + targets, the new jet's window
+  // pass, summaries + the new jet's neighbour; the rapidity chain and the
+  // first detection thread's merge-phase work
+  kPhTRebuild = 12, kPhTS1, kPhTS2, kPhTS3a, kPhTS3b, kPhTS3c, kPhTKin, kPhTDetect, kPhTSteps, kPhTEvents,
+  kPhSlots = 24
 };
 #ifdef FJG_PHASE_CLOCKS
 #define FJG_PH(...) __VA_ARGS__
@@ -386,11 +392,33 @@ __device__ __forceinline__ void move_slot_warp(SmemLayout<T, SPT>& S, const Ws& 
   }
 }
 
+// The new jet's rapidity chain (one lane): its four-momentum (E-scheme,
+// tri_matrix.cu:247-252) and rapidity into slot a, and its label.
+template <int T, int SPT>
+__device__ __forceinline__ void merge_rapidity(SmemLayout<T, SPT>& S, const Ws& g, int a, double pxc, double pyc,
+                                               double pzc, double Ec, double pxj, double pyj, double pzj, double Ej,
+                                               int label) {
+  const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
+  const double pz = __dadd_rn(pzc, pzj), E = __dadd_rn(Ec, Ej);
+  const double rap = fjk_rap(px, py, pz, E);
+  g.at(kPx, a) = px;
+  g.at(kPy, a) = py;
+  g.at(kPz, a) = pz;
+  g.at(kE, a) = E;
+  g.at(kRap, a) = rap;
+  S.rap32[a] = fjk_to_f32(rap, 0);
+  S.label[a] = label;
+}
+
 template <int T, int SPT>
 __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, int e) {
   constexpr int W = T / 32;
   constexpr int MW = (T >= 128) ? 3 : 1;  // merge warps
   constexpr int TR = T - 32 * MW;         // rescan threads
+  // With 64 threads (one merge warp, one rescan warp) the rescan warp takes
+  // the rapidity chain before its scans, so that the merge warp runs only the
+  // azimuth and weight chains instead of all three one after the other.
+  constexpr bool kSplitRap = (MW == 1 && T == 64);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t off;
   EventCtx X;
@@ -631,9 +659,9 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       // Merge warps.  With three: warp 0 computes the azimuth, warp 1 the
       // rapidity and four-momentum, warp 2 the weight and the history record
       // and then compacts (its chain is the shortest); with one, warp 0 does
-      // all of it.  Everything read
-      // of slots c and j is read before barrier 2 (or before the compaction):
-      // the compaction may overwrite one of those slots.
+      // all of it but the rapidity when the CTA has 64 threads (kSplitRap).
+      // Everything read of slots c and j is read before barrier 2 (or before
+      // the compaction): the compaction may overwrite one of those slots.
       const int role = (MW == 1) ? -1 : warp;
       double pxc = 0, pyc = 0, pzc = 0, Ec = 0, pxj = 0, pyj = 0, pzj = 0, Ej = 0;
       double rc = 0, fc = 0, wc = 0, rj = 0, fj = 0, wj = 0;
@@ -660,9 +688,11 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       }
       __syncwarp();
       if (MW > 1) named_sync(2, 32 * MW);  // every merge warp holds its inputs
+      else if (kSplitRap && pair) named_sync(2, T);  // and the rescan warp its own
       FJG_PH(const long long pk0 = clock64();)
       const int lo_l = pair ? min(lc, lj) : lc, hi_l = max(lc, lj);
-      const bool phi_role = role <= 0, rap_role = role == -1 || role == 1, w_role = role == -1 || role == 2;
+      const bool phi_role = role <= 0, rap_role = (role == -1 && !kSplitRap) || role == 1,
+                 w_role = role == -1 || role == 2;
       if (pair) {
         const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
         if (lane == 0 && phi_role) {
@@ -670,17 +700,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
           g.at(kPhi, a) = phi;
           S.phi32[a] = fjk_to_f32(phi, 0);
         }
-        if (lane == 0 && rap_role) {
-          const double pz = __dadd_rn(pzc, pzj), E = __dadd_rn(Ec, Ej);
-          const double rap = fjk_rap(px, py, pz, E);
-          g.at(kPx, a) = px;
-          g.at(kPy, a) = py;
-          g.at(kPz, a) = pz;
-          g.at(kE, a) = E;
-          g.at(kRap, a) = rap;
-          S.rap32[a] = fjk_to_f32(rap, 0);
-          S.label[a] = lo_l;
-        }
+        if (lane == 0 && rap_role) merge_rapidity<T, SPT>(S, g, a, pxc, pyc, pzc, Ec, pxj, pyj, pzj, Ej, lo_l);
         if (lane == 0 && w_role) {
           const double w = fjk_weight(px, py, X.algo);
           g.at(kW, a) = w;
@@ -708,6 +728,27 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       }
       __syncwarp();
     } else {
+      if (kSplitRap && pair) {
+        // the rapidity chain (see kSplitRap): inputs read before barrier 2,
+        // after which the merge warp may compact
+        double pxc = 0, pyc = 0, pzc = 0, Ec = 0, pxj = 0, pyj = 0, pzj = 0, Ej = 0;
+        int lo_l = 0;
+        if (lane == 0) {
+          pxc = g.at(kPx, c);
+          pyc = g.at(kPy, c);
+          pzc = g.at(kPz, c);
+          Ec = g.at(kE, c);
+          pxj = g.at(kPx, j);
+          pyj = g.at(kPy, j);
+          pzj = g.at(kPz, j);
+          Ej = g.at(kE, j);
+          lo_l = min((int)S.label[c], (int)S.label[j]);
+        }
+        __syncwarp();
+        named_sync(2, T);
+        if (lane == 0) merge_rapidity<T, SPT>(S, g, a, pxc, pyc, pzc, Ec, pxj, pyj, pzj, Ej, lo_l);
+        __syncwarp();
+      }
       // Rescan targets: final slots (slot L moves to b) whose neighbour was c or
       // j.  While the merge warps write slots a and b, these warps read
       // neither: data of final slot u is read from src(u) (= L for u == b), and

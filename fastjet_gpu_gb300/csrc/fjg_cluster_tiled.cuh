@@ -732,8 +732,11 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   // ---- clustering steps
   int n = N;
   int step = 0;
+  FJG_PH(long long ph_rb = 0, ph_s1 = 0, ph_s2 = 0, ph_s3a = 0, ph_s3b = 0, ph_s3c = 0, ph_kin = 0, ph_det = 0;)
   while (n > 0) {
+    FJG_PH(const long long ph0 = clock64();)
     if (step > 0 && step % S.slack == 0) rebuild_tiles(S, L, N);
+    FJG_PH(const long long phr = clock64(); ph_rb += phr - ph0;)
 
     // S1: argmin over the tile summaries (slot order breaks ties)
     Cand mine = cand_empty();
@@ -783,6 +786,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     }
 
     // S2
+    FJG_PH(const long long ph1 = clock64(); ph_s1 += ph1 - phr;)
     const bool pair = L.pair[c] != 0 && L.nn[c] >= 0;
     const int j = pair ? L.nn[c] : -1;
     const int a = pair ? min(c, j) : -1;
@@ -812,6 +816,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       }
       __syncwarp();
       named_sync(2, 32 * MW);  // every merge warp has read c and j
+      FJG_PH(const long long pk0 = clock64();)
       if (pair) {
         const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
         if (lane == 0 && warp == 0) {
@@ -852,6 +857,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
         if (A.owner) A.owner[off + c] = -(nj + 1);
         S.ctl_njets = nj + 1;
       }
+      FJG_PH(if (lane == 0) ph_kin += clock64() - pk0;)  // warp 1's (the rapidity chain) is reported
       __syncwarp();
     } else {
       // targets: live slots other than c, j whose neighbour is c or j; they
@@ -898,8 +904,10 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           if (lane == 0) S.rcert[r][warp] = wc;
         }
       }
+      FJG_PH(if (r0 == 0) ph_det += clock64() - ph1;)
     }
     __syncthreads();  // B2
+    FJG_PH(const long long ph2 = clock64(); ph_s2 += ph2 - ph1;)
     --n;
     ++step;
     if (n == 0) break;
@@ -985,6 +993,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       __syncthreads();
     }
 
+    FJG_PH(const long long ph3 = clock64(); ph_s3a += ph3 - ph2;)
     // S3b: every slot of the new jet's window against the new jet
     if (pair) {
       Cert ca = cert_empty();
@@ -1045,6 +1054,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       if (lane == 0) S.wcert[warp] = wc;
     }
     __syncthreads();  // B4
+    FJG_PH(const long long ph4 = clock64(); ph_s3b += ph4 - ph3;)
     // S3c: the new jet's neighbour (warp 0, then its tile's summary) and the
     // other changed tiles' summaries (the remaining warps)
     const int nd = S.n_dirty;
@@ -1074,6 +1084,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       }
     }
     __syncthreads();  // B5
+    FJG_PH(ph_s3c += clock64() - ph4;)
     if (nd > kMaxDirty) {
       for (int k = tid; k < kMaxTiles / 32; k += T) S.dirty_bits[k] = 0;
     } else {
@@ -1090,6 +1101,20 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   // parents (owner[label] = parent label, or -(jet+1) once promoted)
   __syncthreads();
   if (tid == 0) A.n_jets[e] = S.ctl_njets;
+  FJG_PH(if (A.phase) {
+    if (tid == 0) {
+      atomicAdd(A.phase + kPhTRebuild, (unsigned long long)ph_rb);
+      atomicAdd(A.phase + kPhTS1, (unsigned long long)ph_s1);
+      atomicAdd(A.phase + kPhTS2, (unsigned long long)ph_s2);
+      atomicAdd(A.phase + kPhTS3a, (unsigned long long)ph_s3a);
+      atomicAdd(A.phase + kPhTS3b, (unsigned long long)ph_s3b);
+      atomicAdd(A.phase + kPhTS3c, (unsigned long long)ph_s3c);
+      atomicAdd(A.phase + kPhTSteps, (unsigned long long)step);
+      atomicAdd(A.phase + kPhTEvents, 1ull);
+    }
+    if (warp == 1 && lane == 0) atomicAdd(A.phase + kPhTKin, (unsigned long long)ph_kin);
+    if (tid == 32 * MW) atomicAdd(A.phase + kPhTDetect, (unsigned long long)ph_det);
+  })
   if (A.owner) {
     for (int s = tid; s < N; s += T) {
       int x = s, guard = 0;

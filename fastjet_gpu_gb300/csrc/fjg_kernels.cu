@@ -69,30 +69,64 @@ cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
 
 // Events above kSmemMaxN particles go straight to the large list (or raise
 // kStatusTooBig when there is no large workspace, or it is too small).
-// Input check, one warp per event: n_jets[e] = -1 when a momentum component
-// is not finite, when the event's particle range does not lie inside
-// [0, ws_particles) -- the workspace the kernels index by the same offsets --,
-// or when its algorithm code (per-event array) is not kt, C/A or anti-kt or
-// its R (per-event array) is not finite and >= 0 (the event is then refused:
-// kStatusBadArg), else 0.  Events of no or too many particles are left to the
-// bucketing.
-__global__ void k_check_events(const double* p4, int p4_stride, const int64_t* offsets, int n_events,
-                               int32_t* n_jets, int64_t ws_particles, const int32_t* algo, const double* radius) {
-  const int lane = threadIdx.x & 31;
-  const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int e = w0; e < n_events; e += nw) {
+// Input check, in two launches.  k_check_args, one thread per event: n_jets[e]
+// = -1 when the event's particle range does not lie inside [0, ws_particles)
+// -- the workspace the kernels index by the same offsets -- or its algorithm
+// code (per-event array) is not kt, C/A or anti-kt, or its R (per-event array)
+// is not finite and >= 0; else 0.  k_check_moms, a flat pass over every
+// momentum of the batch (16-byte loads where the layout allows): an event with
+// a NaN or infinite component gets n_jets[e] = -1 (its event is found by a
+// binary search of the offsets; such events are rare).  Refused events raise
+// kStatusBadArg in k_size_hist and get no jets.  Events of no or too many
+// particles are left to the bucketing.
+__global__ void k_check_args(const int64_t* offsets, int n_events, int32_t* n_jets, int64_t ws_particles,
+                             const int32_t* algo, const double* radius) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
     const int64_t o0 = offsets[e], o1 = offsets[e + 1];
     bool bad = o1 > o0 && (o0 < 0 || o1 > ws_particles);
     if (algo) bad |= algo[e] < -1 || algo[e] > 1;
     if (radius) bad |= !(radius[e] >= 0.0 && isfinite(radius[e]));
-    if (!bad && o1 - o0 > 0 && o1 - o0 <= kLargeMaxN) {
-      for (int64_t s = o0 + lane; s < o1; s += 32) {
-        const double* p = p4 + s * p4_stride;
-        bad |= !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) && isfinite(p[3]));
-      }
+    n_jets[e] = bad ? -1 : 0;
+  }
+}
+
+__device__ __forceinline__ int event_of(const int64_t* offsets, int n_events, int64_t s) {
+  int lo = 0, hi = n_events - 1;  // the last event with offsets[e] <= s
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= s) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// vec: p4 is [n][4] doubles on a 16-byte boundary, read as pairs of doubles.
+__global__ void k_check_moms(const double* p4, int p4_stride, const int64_t* offsets, int n_events,
+                             int32_t* n_jets, int64_t ws_particles, int vec) {
+  // the particles of the batch, [offsets[0], offsets[n_events]), inside the workspace
+  int64_t end = offsets[n_events];
+  end = end < ws_particles ? end : ws_particles;
+  const int64_t begin = offsets[0] > 0 ? offsets[0] : 0;
+  if (end <= begin) return;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (vec) {
+    // four independent 16-byte loads in flight per thread and iteration
+    const double2* q = reinterpret_cast<const double2*>(p4);
+    const int64_t lim = 2 * end;
+    for (int64_t i = 2 * begin + first; i < lim; i += 4 * stride) {
+      double2 v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = (i + k * stride < lim) ? __ldg(q + i + k * stride) : make_double2(0.0, 0.0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (!(isfinite(v[k].x) && isfinite(v[k].y))) n_jets[event_of(offsets, n_events, (i + k * stride) >> 1)] = -1;
     }
-    bad = __any_sync(0xffffffffu, bad);
-    if (lane == 0) n_jets[e] = bad ? -1 : 0;
+  } else {
+    for (int64_t s = begin + first; s < end; s += stride) {
+      const double* p = p4 + s * p4_stride;
+      if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) && isfinite(p[3])))
+        n_jets[event_of(offsets, n_events, s)] = -1;
+    }
   }
 }
 
@@ -124,7 +158,7 @@ cudaError_t launch_check_pairs(const double* p4, const int64_t* pairs, int n_eve
 __global__ void k_size_hist(const int64_t* offsets, int n_events, int32_t* hist, int32_t* n_jets, int* status,
                             int32_t* large_order, int32_t* large_count, int64_t large_particles) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
-    if (n_jets[e] < 0) {  // non-finite input (k_check_events); k_size_scatter resets it
+    if (n_jets[e] < 0) {  // refused by the input check (k_check_args, k_check_moms); k_size_scatter resets it
       atomicOr(status, kStatusBadArg);
       continue;
     }
@@ -241,15 +275,30 @@ __global__ void k_size_scatter(const int64_t* offsets, int n_events, int32_t* hi
   }
 }
 
+// Blocks of the momentum check: a few per SM, enough 16-byte loads in flight
+// to approach the HBM bandwidth, grid-stride over the rest.
+static int check_grid() {
+  static int cache[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev];
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 132;
+  const int g = 8 * sms;
+  if (dev >= 0 && dev < 64) cache[dev] = g;
+  return g;
+}
+
 static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_events, cudaStream_t stream) {
   cudaError_t err;
   if ((err = cudaMemsetAsync(sc.hist, 0, sizeof(int32_t) * kHistBins, stream)) != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumQueues, stream)) != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(sc.counts + kLargeQueue, 0, sizeof(int32_t), stream)) != cudaSuccess) return err;
   const int grid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
-  const int cgrid = n_events / 8 + 1 > 2048 ? 2048 : n_events / 8 + 1;  // 8 events (warps) per block
-  k_check_events<<<cgrid, 256, 0, stream>>>(base.p4, base.p4_stride, base.offsets, n_events, base.n_jets,
-                                            sc.ws_stride, base.algo, base.radius);
+  k_check_args<<<grid, 256, 0, stream>>>(base.offsets, n_events, base.n_jets, sc.ws_stride, base.algo, base.radius);
+  const int vec = base.p4_stride == 4 && (reinterpret_cast<uintptr_t>(base.p4) & 15) == 0;
+  k_check_moms<<<check_grid(), 256, 0, stream>>>(base.p4, base.p4_stride, base.offsets, n_events, base.n_jets,
+                                                 sc.ws_stride, vec);
   int32_t* large_order = sc.order + kLargeQueue * sc.cap_events;
   k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status, large_order,
                                         sc.counts + kLargeQueue, sc.large_ws ? sc.large_ws_particles : 0);

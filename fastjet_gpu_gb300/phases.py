@@ -6,10 +6,11 @@ Builds the phase-counter variant of the library (-DFJG_PHASE_CLOCKS, into
 fastjet_gpu_gb300/_lib_phases/; the product build is untouched) and loads it
 in place of the product library.  It then clusters lone events of the given
 sizes, one event per launch (anti-kt R=0.4; the plain path, where a step's
-latency is the event's critical path), and one batch of mixed events of
-50-2000 particles (several CTAs per SM, the throughput path).  For each it
-prints the clock cycles per merge step of each phase, as counted by the
-kernel's clock64() phase counters:
+latency is the event's critical path; above 4096 particles pile-up-like
+events on the tiled kernel), and one batch of mixed events of 50-2000
+particles (several CTAs per SM, the throughput path).  For each it prints the
+clock cycles per merge step of each phase, as counted by the kernels'
+clock64() phase counters.  Shared-memory kernel:
 
   s1_argmin      argmin of the keys, up to its decision (barrier B1)
   s2_merge       the merge: new jet's kinematics || target scans, up to B2
@@ -18,6 +19,13 @@ kernel's clock64() phase counters:
   kin_warp0..2   inside s2_merge: each merge warp's kinematics chain
                  (azimuth; rapidity and momentum; weight and history)
   rescan_s2      inside s2_merge: the first rescan thread's work
+
+Tiled kernel: t_rebuild (tile-list rebuilds, per step), t_s1_argmin (over the
+tile summaries), t_s2_merge_detect (merge || target detection and scans),
+t_s3a_lists_targets, t_s3b_window (the new jet against its window),
+t_s3c_summaries (changed tiles, the new jet's neighbour); inside t_s2:
+t_kin_rapidity (the rapidity chain) and t_detect_s2 (the first detection
+thread's work).
 """
 from __future__ import annotations
 
@@ -28,7 +36,7 @@ import sys
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--sizes", default="200,500,1000,2000,4000")
+    ap.add_argument("--sizes", default="200,500,1000,2000,4000,10000,40000")
     ap.add_argument("--batch", type=int, default=1024, help="events of the mixed batch (0: none)")
     ap.add_argument("--algo", type=int, default=-1)
     ap.add_argument("--radius", type=float, default=0.4)
@@ -43,22 +51,34 @@ def main():
     from fastjet_gpu_gb300 import events as E
 
     ctx = F.Context(0)
-    names = [k for k in F.Context.PHASES if k not in ("steps", "events")]
+    small = ["s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
+             "rescan_s2"]
+    tiled = ["t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3a_lists_targets", "t_s3b_window",
+             "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2"]
     rows = []
 
     def report(tag, c):
-        steps = max(c["steps"], 1)
-        row = {"case": tag, "steps": c["steps"], "events": c["events"]}
-        row.update({k: c[k] / steps for k in names})
-        row["step_total"] = sum(row[k] for k in ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve"))
+        row = {"case": tag}
+        if c["steps"]:
+            steps = c["steps"]
+            row.update({"steps": steps, "events": c["events"]})
+            row.update({k: c[k] / steps for k in small})
+            row["step_total"] = sum(row[k] for k in ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve"))
+            print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in small + ["step_total"]), flush=True)
+        if c["t_steps"]:
+            steps = c["t_steps"]
+            row.update({"t_steps": steps, "t_events": c["t_events"]})
+            row.update({k: c[k] / steps for k in tiled})
+            row["t_step_total"] = sum(row[k] for k in tiled[:6])
+            print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in tiled + ["t_step_total"]), flush=True)
         rows.append(row)
-        print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in names + ["step_total"]), flush=True)
 
     for n in [int(x) for x in args.sizes.split(",") if x]:
-        ev = torch.from_numpy(E.single_event(n, 3, seed=900 + n)).cuda()
+        gen = E.single_event(n, 3, seed=900 + n) if n <= 4096 else E.portable_event(n, 4, seed=900 + n)
+        ev = torch.from_numpy(gen).cuda()
         ctx.cluster_event(ev, args.algo, args.radius)
         ctx.phase_clocks(reset=True)
-        for _ in range(3):
+        for _ in range(3 if n <= 4096 else 1):
             ctx.cluster_event(ev, args.algo, args.radius)
         report(f"lone event, {n} particles", ctx.phase_clocks(reset=True))
     if args.batch:

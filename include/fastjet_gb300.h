@@ -96,12 +96,17 @@ const char* fjg_status_string(fjg_status s);
 fjg_status fjg_ctx_check(fjg_ctx* ctx);
 /* Last error message of the context (or of the calling thread when ctx is NULL). */
 const char* fjg_last_error(const fjg_ctx* ctx);
-/* Per-step phase counters of the shared-memory clustering kernel, summed over
- * the events clustered through this context's batch and one-event calls:
- * out[0..3] clock cycles in the argmin, merge, new-jet and neighbour-resolution
- * phases as the CTA's thread 0 sees them, out[4..6] in the merge warps'
- * kinematics chains, out[7] in the first rescan thread's merge-phase work,
- * out[8] steps, out[9] events (n <= 16 entries).  Only a library built with
+/* Per-step phase counters of the clustering kernels, summed over the events
+ * clustered through this context's batch and one-event calls.  Shared-memory
+ * kernel: out[0..3] clock cycles in the argmin, merge, new-jet and
+ * neighbour-resolution phases as the CTA's thread 0 sees them, out[4..6] in
+ * the merge warps' kinematics chains, out[7] in the first rescan thread's
+ * merge-phase work, out[8] steps, out[9] events.  Tiled kernel (events above
+ * 4096 particles): out[12..17] cycles in the list rebuilds, the argmin, the
+ * merge and target detection, the list update and targets, the new jet's
+ * window pass, the tile summaries; out[18] in the rapidity chain, out[19] in
+ * the first detection thread's merge-phase work, out[20] steps, out[21]
+ * events (n <= 24 entries).  Only a library built with
  * -DFJG_PHASE_CLOCKS (python -m fastjet_gpu_gb300.build --phase-clocks) has
  * them; the product build returns FJG_EINVAL.  Waits for the context stream;
  * `reset` zeroes them.  No counterpart in the reference. */
