@@ -410,15 +410,18 @@ __device__ __forceinline__ void merge_rapidity(SmemLayout<T, SPT>& S, const Ws& 
   S.label[a] = label;
 }
 
-template <int T, int SPT>
+template <int T, int SPT, bool SPLIT = false>
 __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, int e) {
   constexpr int W = T / 32;
   constexpr int MW = (T >= 128) ? 3 : 1;  // merge warps
   constexpr int TR = T - 32 * MW;         // rescan threads
-  // With 64 threads (one merge warp, one rescan warp) the rescan warp takes
-  // the rapidity chain before its scans, so that the merge warp runs only the
-  // azimuth and weight chains instead of all three one after the other.
-  constexpr bool kSplitRap = (MW == 1 && T == 64);
+  // With 64 threads (one merge warp, one rescan warp) and SPLIT, the rescan
+  // warp takes the rapidity chain before its scans, so that the merge warp
+  // runs only the azimuth and weight chains instead of all three one after the
+  // other: shorter steps for a lone event (-16 % at 200 particles).  The
+  // register-capped builds, which pack 10-12 CTAs on an SM for throughput, do
+  // not split: the extra live registers spill there and the batch got slower.
+  constexpr bool kSplitRap = SPLIT && (MW == 1 && T == 64);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t off;
   EventCtx X;
