@@ -19,6 +19,9 @@ clock64() phase counters.  Shared-memory kernel:
   kin_warp0..2   inside s2_merge: each merge warp's kinematics chain
                  (azimuth; rapidity and momentum; weight and history)
   rescan_s2      inside s2_merge: the first rescan thread's work
+  exact_*        FP64 fallbacks per step: argmin not certified, a slot's
+                 closer-than-its-neighbour test, a key's pair-or-beam choice,
+                 a neighbour search whose certificate failed
 
 Tiled kernel: t_rebuild (tile-list rebuilds, per step), t_s1_argmin (over the
 tile summaries), t_s2_merge_detect (merge || target detection and scans),
@@ -64,7 +67,11 @@ def main():
             row.update({"steps": steps, "events": c["events"]})
             row.update({k: c[k] / steps for k in small})
             row["step_total"] = sum(row[k] for k in ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve"))
-            print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in small + ["step_total"]), flush=True)
+            # FP64 fallbacks per step (the FP32 intervals could not decide)
+            row.update({k: c[k] / steps for k in ("exact_argmin", "exact_closer", "exact_key", "exact_nn")})
+            print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in small + ["step_total"]) +
+                  "  per step: " + "  ".join(f"{k} {row[k]:.3f}" for k in
+                                            ("exact_argmin", "exact_closer", "exact_key", "exact_nn")), flush=True)
         if c["t_steps"]:
             steps = c["t_steps"]
             row.update({"t_steps": steps, "t_events": c["t_events"]})

@@ -101,7 +101,9 @@ const char* fjg_last_error(const fjg_ctx* ctx);
  * kernel: out[0..3] clock cycles in the argmin, merge, new-jet and
  * neighbour-resolution phases as the CTA's thread 0 sees them, out[4..6] in
  * the merge warps' kinematics chains, out[7] in the first rescan thread's
- * merge-phase work, out[8] steps, out[9] events.  Tiled kernel (events above
+ * merge-phase work, out[8] steps, out[9] events, out[10], out[11], out[22],
+ * out[23] how many FP64 fallbacks the argmin, the closer-neighbour tests, the
+ * key updates and the neighbour searches took.  Tiled kernel (events above
  * 4096 particles): out[12..17] cycles in the list rebuilds, the argmin, the
  * merge and target detection, the list update and targets, the new jet's
  * window pass, the tile summaries; out[18] in the rapidity chain, out[19] in
