@@ -52,6 +52,10 @@ namespace fjg {
 // time of its S2 work.  At the end of an event they are added to A.phase.
 enum PhaseSlot {
   kPhS1 = 0, kPhS2, kPhS3, kPhTail, kPhKin0, kPhKin1, kPhKin2, kPhRescan, kPhSteps, kPhEvents,
+  // how often the FP32 intervals could not decide and FP64 was evaluated:
+  // the argmin (steps), a slot's "is the new jet closer" test, a key's pair-or-
+  // beam choice, a neighbour search's certificate (slot searches)
+  kPhExactArgmin = 10, kPhExactCloser = 11, kPhExactKey = 22, kPhExactNN = 23,
   // the tiled kernel (events above 4096 particles): rebuild of the tile lists,
   // argmin, merge || target detection, lists + targets, the new jet's window
   // pass, summaries + the new jet's neighbour; the rapidity chain and the
@@ -179,6 +183,9 @@ struct SmemLayout {
   int n_rescan;
   int event;
   int ctl_njets;
+#ifdef FJG_PHASE_CLOCKS
+  unsigned ph_exact[4];  // exact-path counts of the event (argmin, closer, key, neighbour)
+#endif
   double rap_max_w[W];
 };
 
@@ -245,6 +252,7 @@ __device__ __forceinline__ void set_key(SmemLayout<T, SPT>& S, const EventCtx& X
     S.pair[t] = (int8_t)kind;
     return;
   }
+  FJG_PH(atomicAdd(&S.ph_exact[2], 1u);)
   const double wt = X.g.at(kW, t);
   const double dp = pair_distance(wt, X.g.at(kW, nn), dr2_slots(X.g, t, nn), X.inv_r2);
   const bool is_pair = dp < wt;
@@ -281,6 +289,7 @@ __device__ __forceinline__ int resolve_nn(SmemLayout<T, SPT>& S, const EventCtx&
     return c.i1;
   }
   const int lane = threadIdx.x & 31;
+  FJG_PH(if (lane == 0) atomicAdd(&S.ph_exact[3], 1u);)
   unsigned long long bk = ~0ull;
   int bl = 0x7fffffff, bi = -1;
   const float rt = S.rap32[t], pt = S.phi32[t];
@@ -413,7 +422,9 @@ __device__ __forceinline__ void merge_rapidity(SmemLayout<T, SPT>& S, const Ws& 
 template <int T, int SPT, bool SPLIT = false>
 __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, int e) {
   constexpr int W = T / 32;
-  constexpr int MW = (T >= 128) ? 3 : 1;  // merge warps
+  // merge warps: three from 256 threads up; two with 128, so that two warps
+  // (not one) scan for the step's targets; one with 64
+  constexpr int MW = (T >= 256) ? 3 : (T == 128 ? 2 : 1);
   constexpr int TR = T - 32 * MW;         // rescan threads
   // With 64 threads (one merge warp, one rescan warp) and SPLIT, the rescan
   // warp takes the rapidity chain before its scans, so that the merge warp
@@ -463,6 +474,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
   if (tid == 0) {
     S.ctl_njets = 0;
     S.n_rescan = 0;
+    FJG_PH(for (int k = 0; k < 4; ++k) S.ph_exact[k] = 0;)
   }
   __syncthreads();
   rmax = 0.0;
@@ -603,6 +615,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       certified = (c >= 0) && (u1 < m2);
     }
     if (!certified && c >= 0) {
+      FJG_PH(if (tid == 0) ++S.ph_exact[0];)
       // near-tie (every thread takes this branch: same shared inputs): exact
       // keys of all slots whose klo does not exceed the winner's khi
       __syncthreads();  // everyone has read warg
@@ -661,8 +674,9 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
     if (warp < MW) {
       // Merge warps.  With three: warp 0 computes the azimuth, warp 1 the
       // rapidity and four-momentum, warp 2 the weight and the history record
-      // and then compacts (its chain is the shortest); with one, warp 0 does
-      // all of it but the rapidity when the CTA has 64 threads (kSplitRap).
+      // and then compacts (its chain is the shortest); with two, warp 0 takes
+      // the azimuth and then warp 2's part; with one, warp 0 does all of it
+      // but the rapidity when the CTA has 64 threads (kSplitRap).
       // Everything read of slots c and j is read before barrier 2 (or before
       // the compaction): the compaction may overwrite one of those slots.
       const int role = (MW == 1) ? -1 : warp;
@@ -695,7 +709,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       FJG_PH(const long long pk0 = clock64();)
       const int lo_l = pair ? min(lc, lj) : lc, hi_l = max(lc, lj);
       const bool phi_role = role <= 0, rap_role = (role == -1 && !kSplitRap) || role == 1,
-                 w_role = role == -1 || role == 2;
+                 w_role = role == -1 || role == 2 || (MW == 2 && role == 0);
       if (pair) {
         const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
         if (lane == 0 && phi_role) {
@@ -820,6 +834,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       } else if (lo > nhi) {
         closer = false;
       } else {
+        FJG_PH(atomicAdd(&S.ph_exact[1], 1u);)
         const double da = dr2_slots(g, t, a);
         const double dc = dr2_slots(g, t, cn);
         closer = da < dc || (da == dc && S.label[a] < S.label[cn]);
@@ -902,6 +917,10 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       atomicAdd(A.phase + kPhTail, (unsigned long long)ph_tail);
       atomicAdd(A.phase + kPhSteps, (unsigned long long)step);
       atomicAdd(A.phase + kPhEvents, 1ull);
+      atomicAdd(A.phase + kPhExactArgmin, (unsigned long long)S.ph_exact[0]);
+      atomicAdd(A.phase + kPhExactCloser, (unsigned long long)S.ph_exact[1]);
+      atomicAdd(A.phase + kPhExactKey, (unsigned long long)S.ph_exact[2]);
+      atomicAdd(A.phase + kPhExactNN, (unsigned long long)S.ph_exact[3]);
     }
     if (warp < MW && lane == 0) atomicAdd(A.phase + kPhKin0 + warp, (unsigned long long)ph_kin);
     if (tid == 32 * MW) atomicAdd(A.phase + kPhRescan, (unsigned long long)ph_resc);
