@@ -233,14 +233,15 @@ class Context:
     PHASES = ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
               "rescan_s2", "steps", "events", "exact_argmin", "exact_closer",
               "t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3a_lists_targets", "t_s3b_window",
-              "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2", "t_steps", "t_events", "exact_key", "exact_nn")
+              "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2", "t_steps", "t_events", "exact_key", "exact_nn",
+              "t_targets", "t_target_steps")
 
     def phase_clocks(self, reset=False):
         """Per-step phase counters of the clustering kernels (only in the
         -DFJG_PHASE_CLOCKS build, see fastjet_gpu_gb300.phases): a dict of
         summed clock cycles per phase, steps and events (t_*: tiled kernel)."""
-        buf = (ctypes.c_ulonglong * 24)()
-        self._check(lib().fjg_phase_clocks(self._h, buf, 24, 1 if reset else 0))
+        buf = (ctypes.c_ulonglong * 32)()
+        self._check(lib().fjg_phase_clocks(self._h, buf, 32, 1 if reset else 0))
         return {k: int(buf[i]) for i, k in enumerate(self.PHASES) if k}
 
     def _after_torch(self, device):

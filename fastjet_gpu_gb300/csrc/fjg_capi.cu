@@ -221,6 +221,7 @@ fjg_status fjg_cluster_batch(fjg_ctx* ctx, const double* p4, const int64_t* offs
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   BatchArgs A{};
   A.phase = ctx->phase;
+  A.particles = total;
   A.p4 = p4;
   A.p4_stride = 4;
   A.offsets = offsets;

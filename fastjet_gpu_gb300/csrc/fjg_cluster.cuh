@@ -61,7 +61,9 @@ enum PhaseSlot {
   // pass, summaries + the new jet's neighbour; the rapidity chain and the
   // first detection thread's merge-phase work
   kPhTRebuild = 12, kPhTS1, kPhTS2, kPhTS3a, kPhTS3b, kPhTS3c, kPhTKin, kPhTDetect, kPhTSteps, kPhTEvents,
-  kPhSlots = 24
+  // the tiled kernel's targets: summed over steps, and steps that had any
+  kPhTTargets = 24, kPhTTargetSteps,
+  kPhSlots = 32
 };
 #ifdef FJG_PHASE_CLOCKS
 #define FJG_PH(...) __VA_ARGS__
@@ -106,6 +108,8 @@ struct BatchArgs {
   int32_t* ev_status;      // null, or per-event status bits: an event whose word is set on entry is
                            // skipped (refused, no jets); bits a kernel raises for event e land here too
   unsigned long long* phase;  // [kPhSlots] phase counters (FJG_PHASE_CLOCKS builds only), or null
+  int64_t particles;       // batch launcher: particles of the p4 buffer (the caller's `total`); the input
+                           // check refuses events that reach past it and reads no momentum beyond it
 };
 
 // Status bits raised by kernels (ORed into the device status word).
@@ -419,20 +423,13 @@ __device__ __forceinline__ void merge_rapidity(SmemLayout<T, SPT>& S, const Ws& 
   S.label[a] = label;
 }
 
-template <int T, int SPT, bool SPLIT = false>
+template <int T, int SPT>
 __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, int e) {
   constexpr int W = T / 32;
   // merge warps: three from 256 threads up; two with 128, so that two warps
   // (not one) scan for the step's targets; one with 64
   constexpr int MW = (T >= 256) ? 3 : (T == 128 ? 2 : 1);
   constexpr int TR = T - 32 * MW;         // rescan threads
-  // With 64 threads (one merge warp, one rescan warp) and SPLIT, the rescan
-  // warp takes the rapidity chain before its scans, so that the merge warp
-  // runs only the azimuth and weight chains instead of all three one after the
-  // other: shorter steps for a lone event (-16 % at 200 particles).  The
-  // register-capped builds, which pack 10-12 CTAs on an SM for throughput, do
-  // not split: the extra live registers spill there and the batch got slower.
-  constexpr bool kSplitRap = SPLIT && (MW == 1 && T == 64);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t off;
   EventCtx X;
@@ -675,8 +672,7 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       // Merge warps.  With three: warp 0 computes the azimuth, warp 1 the
       // rapidity and four-momentum, warp 2 the weight and the history record
       // and then compacts (its chain is the shortest); with two, warp 0 takes
-      // the azimuth and then warp 2's part; with one, warp 0 does all of it
-      // but the rapidity when the CTA has 64 threads (kSplitRap).
+      // the azimuth and then warp 2's part; with one, warp 0 does all of it.
       // Everything read of slots c and j is read before barrier 2 (or before
       // the compaction): the compaction may overwrite one of those slots.
       const int role = (MW == 1) ? -1 : warp;
@@ -705,10 +701,9 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       }
       __syncwarp();
       if (MW > 1) named_sync(2, 32 * MW);  // every merge warp holds its inputs
-      else if (kSplitRap && pair) named_sync(2, T);  // and the rescan warp its own
       FJG_PH(const long long pk0 = clock64();)
       const int lo_l = pair ? min(lc, lj) : lc, hi_l = max(lc, lj);
-      const bool phi_role = role <= 0, rap_role = (role == -1 && !kSplitRap) || role == 1,
+      const bool phi_role = role <= 0, rap_role = role == -1 || role == 1,
                  w_role = role == -1 || role == 2 || (MW == 2 && role == 0);
       if (pair) {
         const double px = __dadd_rn(pxc, pxj), py = __dadd_rn(pyc, pyj);
@@ -745,27 +740,6 @@ __device__ void cluster_event_smem(SmemLayout<T, SPT>& S, const BatchArgs& A, in
       }
       __syncwarp();
     } else {
-      if (kSplitRap && pair) {
-        // the rapidity chain (see kSplitRap): inputs read before barrier 2,
-        // after which the merge warp may compact
-        double pxc = 0, pyc = 0, pzc = 0, Ec = 0, pxj = 0, pyj = 0, pzj = 0, Ej = 0;
-        int lo_l = 0;
-        if (lane == 0) {
-          pxc = g.at(kPx, c);
-          pyc = g.at(kPy, c);
-          pzc = g.at(kPz, c);
-          Ec = g.at(kE, c);
-          pxj = g.at(kPx, j);
-          pyj = g.at(kPy, j);
-          pzj = g.at(kPz, j);
-          Ej = g.at(kE, j);
-          lo_l = min((int)S.label[c], (int)S.label[j]);
-        }
-        __syncwarp();
-        named_sync(2, T);
-        if (lane == 0) merge_rapidity<T, SPT>(S, g, a, pxc, pyc, pzc, Ec, pxj, pyj, pzj, Ej, lo_l);
-        __syncwarp();
-      }
       // Rescan targets: final slots (slot L moves to b) whose neighbour was c or
       // j.  While the merge warps write slots a and b, these warps read
       // neither: data of final slot u is read from src(u) (= L for u == b), and

@@ -732,7 +732,8 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   // ---- clustering steps
   int n = N;
   int step = 0;
-  FJG_PH(long long ph_rb = 0, ph_s1 = 0, ph_s2 = 0, ph_s3a = 0, ph_s3b = 0, ph_s3c = 0, ph_kin = 0, ph_det = 0;)
+  FJG_PH(long long ph_rb = 0, ph_s1 = 0, ph_s2 = 0, ph_s3a = 0, ph_s3b = 0, ph_s3c = 0, ph_kin = 0, ph_det = 0;
+         long long ph_tg = 0, ph_tgs = 0;)
   while (n > 0) {
     FJG_PH(const long long ph0 = clock64();)
     if (step > 0 && step % S.slack == 0) rebuild_tiles(S, L, N);
@@ -912,6 +913,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     ++step;
     if (n == 0) break;
     const int n_found = S.n_rescan;
+    FJG_PH(ph_tg += n_found; ph_tgs += n_found > 0;)
     const int nr_all = min(n_found, kMaxListed);
     const int nr = min(nr_all, kTiledTargets);
     const int ta = pair ? S.ta_u * S.nphi + S.ta_v : -1;
@@ -919,26 +921,34 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     // S3a: tile lists (thread 0: a tombstone for b, and for a when it
     // changes tile, then an append); targets (one warp each)
     if (tid == 0) {
+      // every word the update reads is loaded before its first store: the
+      // arrays are distinct, but the compiler cannot know that the stores to
+      // the member lists leave them alone, and would otherwise wait for each
+      // store before the next load (two L2 round trips instead of four)
+      const int tb = L.tile[b], pb = L.pos[b];
+      const int told = pair ? L.tile[a] : -1, pa = pair ? L.pos[a] : 0;
+      const int cta = pair ? L.t_count[ta] : 0, sta = pair ? L.t_start[ta] : 0;
+      const int sb = L.t_start[tb];
+      const int sold = pair ? L.t_start[told] : 0;
       if (pair) atomicSub(&L.rc[a], S.rc_a_old);
       if (S.rc_drop >= 0) atomicSub(&L.rc[S.rc_drop], 1);
-      L.members[L.t_start[L.tile[b]] + L.pos[b]] = -1;
+      L.members[sb + pb] = -1;
       L.alive[b] = 0;
-      mark_dirty(S, L.tile[b]);
+      mark_dirty(S, tb);
       if (pair) {
-        const int told = L.tile[a];
         mark_dirty(S, told);
         if (ta != told) {
-          L.members[L.t_start[told] + L.pos[a]] = -1;
-          const int p = L.t_count[ta];
-          L.members[L.t_start[ta] + p] = a;
-          L.pos[a] = p;
+          L.members[sold + pa] = -1;
+          L.members[sta + cta] = a;
+          L.pos[a] = cta;
           L.tile[a] = ta;
-          L.t_count[ta] = p + 1;
+          L.t_count[ta] = cta + 1;
           mark_dirty(S, ta);
         }
       }
     }
-    for (int r = warp; r < nr_all; r += W) {
+    // targets go to warps 1, 2, ... first: warp 0's thread 0 is busy above
+    for (int r = (warp + W - 1) % W; r < nr_all; r += W) {
       const int t = S.rlist[r];
       Cert x = cert_empty();
       if (r < nr)
@@ -1111,6 +1121,8 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       atomicAdd(A.phase + kPhTS3c, (unsigned long long)ph_s3c);
       atomicAdd(A.phase + kPhTSteps, (unsigned long long)step);
       atomicAdd(A.phase + kPhTEvents, 1ull);
+      atomicAdd(A.phase + kPhTTargets, (unsigned long long)ph_tg);
+      atomicAdd(A.phase + kPhTTargetSteps, (unsigned long long)ph_tgs);
     }
     if (warp == 1 && lane == 0) atomicAdd(A.phase + kPhTKin, (unsigned long long)ph_kin);
     if (tid == 32 * MW) atomicAdd(A.phase + kPhTDetect, (unsigned long long)ph_det);

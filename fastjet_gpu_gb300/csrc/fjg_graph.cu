@@ -44,6 +44,7 @@ fjg_status fjg_graph_capture_batch(fjg_ctx* ctx, const double* p4, const int64_t
     return cuda_error(ctx, err, "graph scratch");
   }
   fjg::BatchArgs A{};
+  A.particles = total;
   A.p4 = p4;
   A.p4_stride = 4;
   A.offsets = offsets;

@@ -69,21 +69,23 @@ cudaError_t launch_tiled(const BatchArgs& A, int grid, cudaStream_t s) {
 
 // Events above kSmemMaxN particles go straight to the large list (or raise
 // kStatusTooBig when there is no large workspace, or it is too small).
-// Input check, in two launches.  k_check_args, one thread per event: n_jets[e]
-// = -1 when the event's particle range does not lie inside [0, ws_particles)
-// -- the workspace the kernels index by the same offsets -- or its algorithm
-// code (per-event array) is not kt, C/A or anti-kt, or its R (per-event array)
-// is not finite and >= 0; else 0.  k_check_moms, a flat pass over every
-// momentum of the batch (16-byte loads where the layout allows): an event with
-// a NaN or infinite component gets n_jets[e] = -1 (its event is found by a
-// binary search of the offsets; such events are rare).  Refused events raise
+// Input check, in two launches.  `limit` is the smaller of the caller's
+// particle count (the size of p4) and the workspace the kernels index by the
+// same offsets.  k_check_args, one thread per event: n_jets[e] = -1 when the
+// event's particle range does not lie inside [0, limit), or its algorithm code
+// (per-event array) is not kt, C/A or anti-kt, or its R (per-event array) is
+// not finite and >= 0; else 0.  k_check_moms, a flat pass over every momentum
+// of [offsets[0], min(offsets[n_events], limit)) (16-byte loads where the
+// layout allows): an event with a NaN or infinite component gets n_jets[e] =
+// -1 (its event is found by a binary search of the offsets; such events are
+// rare).  No momentum past `limit` is read, whatever the offsets say.  Refused events raise
 // kStatusBadArg in k_size_hist and get no jets.  Events of no or too many
 // particles are left to the bucketing.
-__global__ void k_check_args(const int64_t* offsets, int n_events, int32_t* n_jets, int64_t ws_particles,
+__global__ void k_check_args(const int64_t* offsets, int n_events, int32_t* n_jets, int64_t limit,
                              const int32_t* algo, const double* radius) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_events; e += gridDim.x * blockDim.x) {
     const int64_t o0 = offsets[e], o1 = offsets[e + 1];
-    bool bad = o1 > o0 && (o0 < 0 || o1 > ws_particles);
+    bool bad = o1 > o0 && (o0 < 0 || o1 > limit);
     if (algo) bad |= algo[e] < -1 || algo[e] > 1;
     if (radius) bad |= !(radius[e] >= 0.0 && isfinite(radius[e]));
     n_jets[e] = bad ? -1 : 0;
@@ -101,10 +103,10 @@ __device__ __forceinline__ int event_of(const int64_t* offsets, int n_events, in
 
 // vec: p4 is [n][4] doubles on a 16-byte boundary, read as pairs of doubles.
 __global__ void k_check_moms(const double* p4, int p4_stride, const int64_t* offsets, int n_events,
-                             int32_t* n_jets, int64_t ws_particles, int vec) {
-  // the particles of the batch, [offsets[0], offsets[n_events]), inside the workspace
+                             int32_t* n_jets, int64_t limit, int vec) {
+  // the particles of the batch, [offsets[0], offsets[n_events]), inside p4 and the workspace
   int64_t end = offsets[n_events];
-  end = end < ws_particles ? end : ws_particles;
+  end = end < limit ? end : limit;
   const int64_t begin = offsets[0] > 0 ? offsets[0] : 0;
   if (end <= begin) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -295,10 +297,11 @@ static cudaError_t launch_sort(const BatchArgs& base, const Scratch& sc, int n_e
   if ((err = cudaMemsetAsync(sc.queues, 0, sizeof(int) * kNumQueues, stream)) != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(sc.counts + kLargeQueue, 0, sizeof(int32_t), stream)) != cudaSuccess) return err;
   const int grid = (n_events + 255) / 256 < 1 ? 1 : ((n_events + 255) / 256 > 1024 ? 1024 : (n_events + 255) / 256);
-  k_check_args<<<grid, 256, 0, stream>>>(base.offsets, n_events, base.n_jets, sc.ws_stride, base.algo, base.radius);
+  const int64_t limit = base.particles < sc.ws_stride ? base.particles : sc.ws_stride;
+  k_check_args<<<grid, 256, 0, stream>>>(base.offsets, n_events, base.n_jets, limit, base.algo, base.radius);
   const int vec = base.p4_stride == 4 && (reinterpret_cast<uintptr_t>(base.p4) & 15) == 0;
   k_check_moms<<<check_grid(), 256, 0, stream>>>(base.p4, base.p4_stride, base.offsets, n_events, base.n_jets,
-                                                 sc.ws_stride, vec);
+                                                 limit, vec);
   int32_t* large_order = sc.order + kLargeQueue * sc.cap_events;
   k_size_hist<<<grid, 256, 0, stream>>>(base.offsets, n_events, sc.hist, base.n_jets, sc.status, large_order,
                                         sc.counts + kLargeQueue, sc.large_ws ? sc.large_ws_particles : 0);

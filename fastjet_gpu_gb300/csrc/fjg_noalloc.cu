@@ -21,8 +21,8 @@
 // streams or host threads without ordering) race on it.
 //
 // Bounds: the input check refuses events whose range [offsets[e],
-// offsets[e+1]) leaves [0, kNoAllocMaxParticles), the extent of the
-// per-particle workspace.  An event above 4096 particles uses
+// offsets[e+1]) leaves [0, total) (total <= kNoAllocMaxParticles, the extent
+// of the per-particle workspace) and reads no momentum past `total`.  An event above 4096 particles uses
 // large_ws_bytes(N) <= 91 N + 31 < kLargeWsBytesPerParticle * N bytes from
 // kLargeWsBytesPerParticle * offsets[e] on, so its region ends inside the
 // large workspace too (no margin is needed past the last particle).
@@ -116,6 +116,7 @@ extern "C" fjg_status fjg_cluster_batch_noalloc(const double* p4, const int64_t*
   sc.large_ws_particles = kNoAllocMaxParticles;
 
   fjg::BatchArgs A{};
+  A.particles = total;
   A.p4 = p4;
   A.p4_stride = 4;
   A.offsets = offsets;

@@ -86,6 +86,7 @@ struct TuneBuffers {
 cudaError_t time_batch(fjg_ctx* ctx, const TuneBuffers& tb, int n_events, int64_t total, int algo, double r,
                        const fjg::Tuning& t, double* seconds) {
   fjg::BatchArgs A{};
+  A.particles = total;
   A.p4 = tb.p4;
   A.p4_stride = 4;
   A.offsets = tb.off;

@@ -14,7 +14,7 @@
 
 namespace fjg {
 
-template <int T, int SPT, bool SPLIT>
+template <int T, int SPT>
 __device__ __forceinline__ void smem_event_loop(const BatchArgs& A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SmemLayout<T, SPT>& S = *reinterpret_cast<SmemLayout<T, SPT>*>(smem_raw);
@@ -28,19 +28,19 @@ __device__ __forceinline__ void smem_event_loop(const BatchArgs& A) {
     const int e = S.event;
     if (e < 0) break;
     if (refused_event(A, e)) continue;  // ends with a barrier
-    cluster_event_smem<T, SPT, SPLIT>(S, A, e);  // ends with a barrier
+    cluster_event_smem<T, SPT>(S, A, e);  // ends with a barrier
     if (threadIdx.x == 0) signal_done(A, e);
   }
 }
 
 template <int T, int SPT>
 __global__ void __launch_bounds__(T) k_cluster_smem(BatchArgs A) {
-  smem_event_loop<T, SPT, true>(A);
+  smem_event_loop<T, SPT>(A);
 }
 
 template <int T, int SPT, int MINB>
 __global__ void __launch_bounds__(T, MINB) k_cluster_smem_capped(BatchArgs A) {
-  smem_event_loop<T, SPT, false>(A);
+  smem_event_loop<T, SPT>(A);
 }
 
 // Dynamic shared memory attribute, set once per device and kernel.

@@ -77,7 +77,11 @@ def main():
             row.update({"t_steps": steps, "t_events": c["t_events"]})
             row.update({k: c[k] / steps for k in tiled})
             row["t_step_total"] = sum(row[k] for k in tiled[:6])
-            print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in tiled + ["t_step_total"]), flush=True)
+            row["t_targets_per_step"] = c["t_targets"] / steps
+            row["t_steps_with_targets"] = c["t_target_steps"] / steps
+            print(f"{tag:>28}: " + "  ".join(f"{k} {row[k]:8.0f}" for k in tiled + ["t_step_total"]) +
+                  f"  targets per step {row['t_targets_per_step']:.2f}, steps with targets "
+                  f"{row['t_steps_with_targets']:.2f}", flush=True)
         rows.append(row)
 
     for n in [int(x) for x in args.sizes.split(",") if x]:

@@ -108,7 +108,8 @@ const char* fjg_last_error(const fjg_ctx* ctx);
  * merge and target detection, the list update and targets, the new jet's
  * window pass, the tile summaries; out[18] in the rapidity chain, out[19] in
  * the first detection thread's merge-phase work, out[20] steps, out[21]
- * events (n <= 24 entries).  Only a library built with
+ * events, out[24] targets found (slots whose neighbour was merged) and
+ * out[25] steps with any (n <= 32 entries).  Only a library built with
  * -DFJG_PHASE_CLOCKS (python -m fastjet_gpu_gb300.build --phase-clocks) has
  * them; the product build returns FJG_EINVAL.  Waits for the context stream;
  * `reset` zeroes them.  No counterpart in the reference. */
@@ -348,9 +349,9 @@ fjg_status fjg_server_replay(fjg_server* server, const double* p4, const int64_t
  * address.  Every call synchronises `stream` before it returns (it reads the
  * kernels' status word back), so the entry point cannot be used inside stream
  * capture.  Calls share the array: calls whose work overlaps on the GPU race
- * and must be serialised by the caller.  Event ranges outside
- * [0, FJG_NOALLOC_MAX_PARTICLES) are refused (FJG_EINVAL), as are
- * non-finite momenta. */
+ * and must be serialised by the caller.  Event ranges outside [0, total) are
+ * refused (FJG_EINVAL) and their momenta are not read, as are non-finite
+ * momenta. */
 #define FJG_NOALLOC_MAX_EVENTS 65536
 #define FJG_NOALLOC_MAX_PARTICLES 131072
 #define FJG_NOALLOC_SCRATCH_BYTES ((7 * 8 + 96) * FJG_NOALLOC_MAX_PARTICLES + 6 * 4 * FJG_NOALLOC_MAX_EVENTS + 32768)

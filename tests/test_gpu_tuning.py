@@ -150,3 +150,22 @@ def test_autotune_picks_compiled_shapes(ctx):
             assert np.array_equal(a["jets"][o0:o0 + nj], r["jets"][o0:o0 + nj])
     finally:
         c.close()
+
+
+def test_phase_counters_absent_from_product_build():
+    """The per-step phase counters are compiled only into the separate
+    -DFJG_PHASE_CLOCKS build (python -m fastjet_gpu_gb300.phases); the product
+    library reports FJG_EINVAL for them and clusters as usual."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import fastjet_gpu_gb300 as F
+    from fastjet_gpu_gb300 import events as E
+    ctx = F.Context(0)
+    with pytest.raises(F.FjgError) as ei:
+        ctx.phase_clocks()
+    assert ei.value.status == 1 and "FJG_PHASE_CLOCKS" in str(ei.value)
+    b = E.mixed_batch(8, 50, 300, seed=9)
+    res = ctx.cluster_batch(b.particles, b.offsets, -1, 0.4)
+    assert int(res["n_jets"].sum()) > 0
+    ctx.close()
