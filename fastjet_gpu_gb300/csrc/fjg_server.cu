@@ -3,11 +3,14 @@
 //
 // Memory.  An arena of `arena_particles` particle positions.  Each admitted
 // event holds one contiguous range [start, start + n):
-//   pinned, mapped host memory: momenta (written by the host at admission,
-//     read by the kernels directly), jets, jet labels, history and owner
-//     (written by the kernels directly, read by the host on completion);
-//   device memory: the FP64 workspace (kWsFields doubles per position) and
-//     the tiled kernel's workspace (kLargeWsBytesPerParticle per position).
+//   pinned, mapped host memory: the momenta's staging copy (written by the
+//     host at admission), jets, jet labels, history and owner (written by the
+//     kernels directly, read by the host on completion);
+//   device memory: the momenta (copied from the staging range at admission,
+//     on a copy stream that every launch waits for), the FP64 workspace
+//     (kWsFields doubles per position) and the tiled kernel's workspace
+//     (kLargeWsBytesPerParticle per position).  The particle and neighbour
+//     state the kernels read is device-resident.
 // A request also holds a completion slot: a flag in mapped host memory that
 // its kernel raises (system-scope release store) once the event's outputs
 // are written.
@@ -95,7 +98,10 @@ struct fjg_server {
   fjg_server_config cfg{};
   // mapped host arena (host and device views)
   void* host_mem = nullptr;
-  double *h_p4 = nullptr, *d_p4 = nullptr, *h_jets = nullptr, *d_jets = nullptr;
+  double *h_p4 = nullptr, *h_jets = nullptr, *d_jets = nullptr;
+  double* d_p4dev = nullptr;       // device copy of the momenta (arena positions)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copy = nullptr;   // after the last admission's copy
   int32_t *h_lab = nullptr, *d_lab = nullptr, *h_own = nullptr, *d_own = nullptr;
   fjg_step *h_hist = nullptr, *d_hist = nullptr;
   int32_t *h_done = nullptr, *d_done = nullptr;
@@ -191,7 +197,7 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
   }
   *L.host.count = m;
   fjg::BatchArgs A{};
-  A.p4 = S->d_p4;
+  A.p4 = S->d_p4dev;
   A.p4_stride = 4;
   A.offsets = L.dev.offsets;
   A.pairs = 1;
@@ -215,12 +221,14 @@ cudaError_t launch_lane(fjg_server* S, Lane& L, int q, int m) {
   A.done_slot = L.dev.done_slot;
   A.ev_status = L.dev.ev_status;
   L.attributed = 0;
-  cudaError_t err = cudaMemsetAsync(L.d_queue, 0, 2 * sizeof(int), L.stream);  // queue head and status
+  // the momenta of the micro-batch were copied at admission
+  cudaError_t err = cudaStreamWaitEvent(L.stream, S->ev_copy, 0);
+  if (err == cudaSuccess) err = cudaMemsetAsync(L.d_queue, 0, 2 * sizeof(int), L.stream);  // queue head and status
   if (err != cudaSuccess) return err;
   if (S->cfg.flags & FJG_SERVE_DEVICE_CHECK) {
     // momenta checked on the device: a request with a non-finite component
     // gets its own status word set and is skipped by the clustering kernel
-    err = fjg::launch_check_pairs(S->d_p4, L.dev.offsets, m, L.dev.ev_status, L.stream);
+    err = fjg::launch_check_pairs(S->d_p4dev, L.dev.offsets, m, L.dev.ev_status, L.stream);
     if (err != cudaSuccess) return err;
   }
   if (q == fjg::kLargeQueue) {
@@ -273,7 +281,9 @@ bool progress(fjg_server* S) {
     L.busy = false;
     L.batch.clear();
   }
-  // 2. admission (first come, first served)
+  // 2. admission (first come, first served): the momenta go to the staging
+  // range and are copied to the device arena on the copy stream
+  bool copied = false;
   while (!S->pending.empty() && !S->free_slots.empty()) {
     Req* r = S->pending.front();
     const int64_t start = arena_alloc(S, r->n);
@@ -283,12 +293,22 @@ bool progress(fjg_server* S) {
     r->slot = S->free_slots.back();
     S->free_slots.pop_back();
     std::memcpy(S->h_p4 + 4 * start, r->src, sizeof(double) * 4 * (size_t)r->n);
+    if (cudaMemcpyAsync(S->d_p4dev + 4 * start, S->h_p4 + 4 * start, sizeof(double) * 4 * (size_t)r->n,
+                        cudaMemcpyHostToDevice, S->copy_stream) != cudaSuccess) {
+      S->failed = true;
+      return false;
+    }
+    copied = true;
     r->copy.clear();
     r->copy.shrink_to_fit();
     r->src = nullptr;
     __atomic_store_n(&S->h_done[r->slot], 0, __ATOMIC_RELEASE);
     r->state = kAdmitted;
     S->admitted[r->bucket].push_back(r);
+  }
+  if (copied && cudaEventRecord(S->ev_copy, S->copy_stream) != cudaSuccess) {
+    S->failed = true;
+    return false;
   }
   // 3. launches, smallest events first (they are the latency-bound
   // requests); events above 4096 particles take at most half of the streams
@@ -384,7 +404,10 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
   const size_t b_ws = al(sizeof(double) * fjg::kWsFields * (size_t)P);
   const size_t b_large = al((size_t)fjg::kLargeWsBytesPerParticle * (size_t)P);
   const size_t b_iota = al(4 * (size_t)c.max_batch), b_words = al(8 * (size_t)c.streams);
-  if (err == cudaSuccess) err = cudaMalloc(&S->dev_mem, b_ws + b_large + b_iota + b_words);
+  const size_t b_p4dev = al(32 * (size_t)P);
+  if (err == cudaSuccess) err = cudaMalloc(&S->dev_mem, b_ws + b_large + b_iota + b_words + b_p4dev);
+  if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&S->copy_stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&S->ev_copy, cudaEventDisableTiming);
   auto dev_of = [&](void* h) {
     void* d = nullptr;
     if (err == cudaSuccess) err = cudaHostGetDevicePointer(&d, h, 0);
@@ -398,7 +421,6 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
     S->h_hist = hist ? reinterpret_cast<fjg_step*>(h + b_p4 + b_jets + b_lab) : nullptr;
     S->h_own = hist ? reinterpret_cast<int32_t*>(h + b_p4 + b_jets + b_lab + b_hist) : nullptr;
     S->h_done = reinterpret_cast<int32_t*>(h + b_p4 + b_jets + b_lab + b_hist + b_own);
-    S->d_p4 = static_cast<double*>(dev_of(S->h_p4));
     S->d_jets = static_cast<double*>(dev_of(S->h_jets));
     S->d_lab = static_cast<int32_t*>(dev_of(S->h_lab));
     S->d_hist = hist ? static_cast<fjg_step*>(dev_of(S->h_hist)) : nullptr;
@@ -409,6 +431,7 @@ fjg_status fjg_server_create(fjg_ctx* ctx, const fjg_server_config* config, fjg_
     S->d_large = reinterpret_cast<unsigned char*>(d + b_ws);
     S->d_iota = reinterpret_cast<int32_t*>(d + b_ws + b_large);
     S->d_words = reinterpret_cast<int*>(d + b_ws + b_large + b_iota);
+    S->d_p4dev = reinterpret_cast<double*>(d + b_ws + b_large + b_iota + b_words);
     std::memset(S->h_done, 0, 4 * (size_t)c.max_inflight);
   }
   std::vector<int32_t> iota(c.max_batch);
@@ -480,6 +503,11 @@ void fjg_server_destroy(fjg_server* S) {
     for (Req* r : L.batch) delete r;  // entries of completed requests are null
   for (Req* r : S->completed) delete r;
   for (auto& kv : S->returned) delete kv.second;
+  if (S->copy_stream) {
+    cudaStreamSynchronize(S->copy_stream);
+    cudaStreamDestroy(S->copy_stream);
+  }
+  if (S->ev_copy) cudaEventDestroy(S->ev_copy);
   if (S->dev_mem) cudaFree(S->dev_mem);
   if (S->host_mem) cudaFreeHost(S->host_mem);
   if (S->block_mem) cudaFreeHost(S->block_mem);

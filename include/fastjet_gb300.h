@@ -255,10 +255,11 @@ fjg_status fjg_parse_events(const char* text, size_t len, int threads, double* p
  * are submitted one at a time as they arrive and complete independently.
  *
  * - State: a particle arena of `arena_particles` entries.  An admitted event
- *   holds a contiguous range of it: its momenta and results in pinned host
- *   memory that the kernels read and write directly, its clustering state
- *   (the FP64 workspace, and the tiled kernel's workspace above 4096
- *   particles) in device memory.  Admission is first come, first served, by
+ *   holds a contiguous range of it: its momenta are copied into device memory
+ *   as it is admitted (through a pinned staging range) and stay there with its
+ *   clustering state (the FP64 workspace, and the tiled kernel's workspace
+ *   above 4096 particles) while it is clustered; its results go to pinned host
+ *   memory that the kernels write directly.  Admission is first come, first served, by
  *   arena space (the HBM footprint) and by the resident CTA slots of the
  *   event's size bucket (the shared-memory footprint, oversubscribed by at
  *   most `oversubscribe`).
