@@ -79,7 +79,11 @@ namespace fjg {
 
 constexpr int kTiledT = 256;
 constexpr int kListSlack = 64;      // spare list entries per possible tile
-constexpr int kTileSlackMax = 256;  // rebuild interval bound (steps)
+// rebuild interval bound (steps): above what the spare area allows for the
+// event sizes of interest (~870 steps at 40k particles), so that the area, not
+// this bound, sets how rarely the lists are rebuilt (1024 against 256: pile-up
+// batch +4 %, same-box A/B)
+constexpr int kTileSlackMax = 1024;
 constexpr int kMaxTiles = 4096;
 constexpr double kTileMembers = 32.0;  // particles per tile the tile side aims at (at least)
 constexpr int kMaxWindowTiles = 9;
