@@ -85,6 +85,11 @@ constexpr int kListSlack = 64;      // spare list entries per possible tile
 // batch +4 %, same-box A/B)
 constexpr int kTileSlackMax = 1024;
 constexpr int kMaxTiles = 4096;
+// Tiles of one event in use, at most: their list ranges and key summaries live
+// in shared memory (40 KB), so every phase reads them there and not through
+// an L2 round trip.  Events that would want more get coarser tiles (still
+// correct, see above): ~300 tiles at R = 0.4 over |y| < 4.
+constexpr int kSmemTiles = 1024;
 constexpr double kTileMembers = 32.0;  // particles per tile the tile side aims at (at least)
 constexpr int kMaxWindowTiles = 9;
 constexpr int kTiledTargets = 32;                // targets per step scanned during the merge
@@ -167,8 +172,8 @@ struct LargeWs {
   int* rc;                                                    // [N] slots whose neighbour this is
   int8_t *pair, *alive;                                       // [N]
   int* members;                                               // [N + kListSlack * MT]
-  int *t_start, *t_count;                                     // [MT]
-  TileSum* tsum;                                              // [MT]
+  int *t_start, *t_count;                                     // [MT] (the kernel points these
+  TileSum* tsum;                                              // [MT]  three at shared memory)
   int max_tiles;                                              // MT
   int list_cap;                                               // bound of one tile's list length
 };
@@ -230,6 +235,9 @@ struct TiledShared {
   int event, ctl_njets;
   double red[3][W];
   int scan_tmp[W];
+  // the event's tile lists' ranges and the tile summaries (LargeWs points here)
+  int t_start[kSmemTiles], t_count[kSmemTiles];
+  TileSum tsum[kSmemTiles];
 };
 
 __device__ __forceinline__ int tile_u(const TiledShared& S, double rap) {
@@ -601,7 +609,10 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   const Ws& g = X.g;
   const int N = X.N;
   // event e's region starts kLargeWsBytesPerParticle * offsets[e] bytes in
-  const LargeWs L = large_ws(large_base + off * kLargeWsBytesPerParticle, N);
+  LargeWs L = large_ws(large_base + off * kLargeWsBytesPerParticle, N);
+  L.t_start = S.t_start;
+  L.t_count = S.t_count;
+  L.tsum = S.tsum;
 
   // ---- load and kinematics; rapidity range
   double rlo = 1e300, rhi = -1e300, amax = 0.0;
@@ -658,7 +669,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     int nrap = (int)fmin(floor((hi - lo) / side_min), 4096.0);
     nrap = nrap < 1 ? 1 : nrap;
     // coarser tiles are still correct, only slower
-    while (nrap * nphi > L.max_tiles) {
+    while (nrap * nphi > min(L.max_tiles, kSmemTiles)) {
       if (nrap > 1)
         nrap = (nrap + 1) / 2;
       else

@@ -40,9 +40,10 @@ int launch_priority(int level) {
   return p > least ? least : p;
 }
 
-// The tiled kernel keeps its state in global memory and leans on L1 (it has
-// 3.8 KB of shared memory): ask for the largest L1 split, so that it does not
-// run with the small L1 that the shared-memory bucket kernels leave on an SM.
+// The tiled kernel keeps its per-slot state in global memory and leans on L1
+// (its 46 KB of shared memory hold the tile ranges and summaries): ask for the
+// largest L1 split, so that it does not run with the small L1 that the
+// shared-memory bucket kernels leave on an SM.
 cudaError_t configure_tiled() {
   static bool done[64] = {};
   int dev = 0;
