@@ -232,7 +232,7 @@ class Context:
 
     PHASES = ("s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
               "rescan_s2", "steps", "events", "exact_argmin", "exact_closer",
-              "t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3a_lists_targets", "t_s3b_window",
+              "t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3_lists_targets_window", "t_s3_overflow",
               "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2", "t_steps", "t_events", "exact_key", "exact_nn",
               "t_targets", "t_target_steps")
 

@@ -57,9 +57,10 @@ enum PhaseSlot {
   // beam choice, a neighbour search's certificate (slot searches)
   kPhExactArgmin = 10, kPhExactCloser = 11, kPhExactKey = 22, kPhExactNN = 23,
   // the tiled kernel (events above 4096 particles): rebuild of the tile lists,
-  // argmin, merge || target detection, lists + targets, the new jet's window
-  // pass, summaries + the new jet's neighbour; the rapidity chain and the
-  // first detection thread's merge-phase work
+  // argmin, merge || target detection, lists + targets + the new jet's window
+  // pass, the pass for targets beyond the listed ones, summaries + the new
+  // jet's neighbour; the rapidity chain and the first detection thread's
+  // merge-phase work
   kPhTRebuild = 12, kPhTS1, kPhTS2, kPhTS3a, kPhTS3b, kPhTS3c, kPhTKin, kPhTDetect, kPhTSteps, kPhTEvents,
   // the tiled kernel's targets: summed over steps, and steps that had any
   kPhTTargets = 24, kPhTTargetSteps,

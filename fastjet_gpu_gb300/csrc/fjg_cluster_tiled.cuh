@@ -37,8 +37,9 @@
 // (kListSlack entries per possible tile, spread over the tiles in use), at
 // most kTileSlackMax.
 //
-// The update runs on thread 0 in S3a while the other warps scan windows for
-// the step's targets, with no barrier or fence between them.  Its stores, and
+// The update runs on thread 0 in S3 while the other warps scan windows for
+// the step's targets and the new jet's window, with no barrier or fence
+// between them.  Its stores, and
 // what a concurrent reader of the same words can observe (32-bit words, so
 // each load returns the old or the new value, never a mix):
 //   (1) members[start[tile b] + pos b] = -1: the reader sees b or -1;
@@ -50,7 +51,7 @@
 //       last rebuild (counts only grow between rebuilds, by one per append),
 //       so nothing has written it since the rebuild set it to -1;
 //   (4) pos[a], tile[a], alive[b] and the referrer counts of a and of one
-//       dropped neighbour: no S3a reader uses them for a, b or as an index.
+//       dropped neighbour: no S3 reader uses them for a, b or as an index.
 // Every outcome is a, b or -1, and every reader skips -1 and the merged slots
 // c and j by name ({a, b} = {c, j}); the new jet a enters the targets'
 // searches explicitly (`extra`), not through the lists.  So the scans find
@@ -65,12 +66,13 @@
 //   S2  warps 0-2 merge or promote (the new jet's kinematics and tile);
 //       warps 3-7 find the slots whose neighbour was c or j (in the windows
 //       of c's and j's tiles) and scan the first 32 of them.               B2
-//   S3a thread 0 updates the tile lists; the warps finish the targets'
-//       neighbours, adding the new jet when it lies in their window.      B3
+//   S3  thread 0 updates the tile lists; the warps finish the targets'
+//       neighbours, adding the new jet when it lies in their window, and
+//       then compare every slot of the new jet's window with it (targets,
+//       flagged in S2, are left to their own searches).                   B3
 //       (targets beyond the listed ones: a second pass, then a barrier)
-//   S3b every slot of the new jet's window is compared with it.           B4
 //   S3c warp 0 resolves the new jet's neighbour and then re-summarises its
-//       tile; the other warps re-summarise the other changed tiles.       B5
+//       tile; the other warps re-summarise the other changed tiles.       B4
 #pragma once
 
 #include "fjg_cluster.cuh"
@@ -908,6 +910,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
             if (nu[k] == c || (pair && nu[k] == j)) {
               const int p = atomicAdd(&S.n_rescan, 1);
               if (p < kMaxListed) S.rlist[p] = u[k];
+              L.alive[u[k]] = 2;  // a target of this step (cleared after B3)
             }
           }
         }
@@ -989,37 +992,14 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       }
       __syncwarp();
     }
-    __syncthreads();  // B3: lists updated, listed targets done
-    if (n_found > kMaxListed) {
-      // more targets than listed (degenerate inputs, e.g. repeated
-      // particles): find them again with the lists up to date; the listed
-      // ones are found too and get the same answer again
-      int tiles[2 * kMaxWindowTiles];
-      const int nw = window_union(S, tile_c, tile_j, tiles);
-      for (int k = warp; k < nw; k += W) {
-        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
-        for (int i0 = 0; i0 < m; i0 += 32) {
-          const int i = i0 + lane;
-          const int u = (i < m) ? L.members[base + i] : -1;
-          const bool hit = u >= 0 && u != a && u != b && (L.nn[u] == c || (pair && L.nn[u] == j));
-          unsigned ball = __ballot_sync(kFull, hit);
-          while (ball) {
-            const int src = __ffs(ball) - 1;
-            ball &= ball - 1;
-            const int t = __shfl_sync(kFull, u, src);
-            // a listed target whose new neighbour is the new jet in a merged
-            // slot is found again: it is done (and counted) already
-            bool listed = false;
-            for (int q = lane; q < kMaxListed; q += 32) listed |= S.rlist[q] == t;
-            if (!__any_sync(kFull, listed)) rescan_warp(S, L, X, t, b);
-          }
-        }
-      }
-      __syncthreads();
-    }
-
-    FJG_PH(const long long ph3 = clock64(); ph_s3a += ph3 - ph2;)
-    // S3b: every slot of the new jet's window against the new jet
+    // S3b, in the same phase: every slot of the new jet's window against the
+    // new jet, beside the list update and the targets' searches (no barrier
+    // between them).  This step's targets (alive == 2, set before B2) are
+    // compared for the new jet's own search but not updated: their searches
+    // offer them the new jet (`extra`).  Every other slot's neighbour,
+    // intervals and key are written only here, the lists are read as the
+    // targets' scans read them (see "Tile lists"), and the new jet's fields
+    // were written before B2.
     if (pair) {
       Cert ca = cert_empty();
       int tiles[kMaxWindowTiles];
@@ -1028,7 +1008,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       constexpr int NT = kMaxWindowTiles;
       const TileRanges<NT> R = tile_ranges<NT>(L, tiles, nw);
       for (int i = tid; i < R.maxlen; i += T) {
-        int u[NT], cn[NT];
+        int u[NT], cn[NT], al[NT];
         float r[NT], ph[NT], nl[NT], nh[NT];
 #pragma unroll
         for (int k = 0; k < NT; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
@@ -1040,6 +1020,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
             cn[k] = L.nn[u[k]];
             nl[k] = L.nlo[u[k]];
             nh[k] = L.nhi[u[k]];
+            al[k] = L.alive[u[k]];
           }
         }
 #pragma unroll
@@ -1049,7 +1030,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           float lo, hi;
           dr2_32(r[k], ph[k], ra, pa, X.bd, lo, hi);
           cert_add(ca, lo, hi, t);
-          if (cn[k] == a) continue;
+          if (cn[k] == a || al[k] == 2) continue;
           bool closer;
           float ulo = lo, uhi = hi;
           if (cn[k] < 0 || hi < nl[k]) {
@@ -1078,7 +1059,37 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       const Cert wc = cert_warp(ca);
       if (lane == 0) S.wcert[warp] = wc;
     }
-    __syncthreads();  // B4
+    __syncthreads();  // B3: lists updated, listed targets done, the new jet's window compared
+    FJG_PH(const long long ph3 = clock64(); ph_s3a += ph3 - ph2;)
+    if (n_found > kMaxListed) {
+      // more targets than listed (degenerate inputs, e.g. repeated
+      // particles): the unlisted ones (still flagged) are searched again
+      // with the lists up to date, which offers them the new jet
+      int tiles[2 * kMaxWindowTiles];
+      const int nw = window_union(S, tile_c, tile_j, tiles);
+      for (int k = warp; k < nw; k += W) {
+        const int base = L.t_start[tiles[k]], m = L.t_count[tiles[k]];
+        for (int i0 = 0; i0 < m; i0 += 32) {
+          const int i = i0 + lane;
+          const int u = (i < m) ? L.members[base + i] : -1;
+          const bool hit = u >= 0 && u != a && u != b && L.alive[u] == 2;
+          unsigned ball = __ballot_sync(kFull, hit);
+          while (ball) {
+            const int src = __ffs(ball) - 1;
+            ball &= ball - 1;
+            const int t = __shfl_sync(kFull, u, src);
+            bool listed = false;
+            for (int q = lane; q < kMaxListed; q += 32) listed |= S.rlist[q] == t;
+            if (!__any_sync(kFull, listed)) {
+              rescan_warp(S, L, X, t, b);
+              if (lane == 0) L.alive[t] = 1;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    for (int r = tid; r < nr_all; r += T) L.alive[S.rlist[r]] = 1;  // the listed targets' flags
     FJG_PH(const long long ph4 = clock64(); ph_s3b += ph4 - ph3;)
     // S3c: the new jet's neighbour (warp 0, then its tile's summary) and the
     // other changed tiles' summaries (the remaining warps)
@@ -1108,7 +1119,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           if (S.dirty[k] != ta) tile_summary(L, S.dirty[k]);
       }
     }
-    __syncthreads();  // B5
+    __syncthreads();  // B4
     FJG_PH(ph_s3c += clock64() - ph4;)
     if (nd > kMaxDirty) {
       for (int k = tid; k < kMaxTiles / 32; k += T) S.dirty_bits[k] = 0;

@@ -25,8 +25,8 @@ clock64() phase counters.  Shared-memory kernel:
 
 Tiled kernel: t_rebuild (tile-list rebuilds, per step), t_s1_argmin (over the
 tile summaries), t_s2_merge_detect (merge || target detection and scans),
-t_s3a_lists_targets, t_s3b_window (the new jet against its window),
-t_s3c_summaries (changed tiles, the new jet's neighbour); inside t_s2:
+t_s3_lists_targets_window (list update, targets, the new jet against its
+window), t_s3_overflow (targets beyond the listed ones, flags), t_s3c_summaries (changed tiles, the new jet's neighbour); inside t_s2:
 t_kin_rapidity (the rapidity chain) and t_detect_s2 (the first detection
 thread's work).
 """
@@ -56,7 +56,7 @@ def main():
     ctx = F.Context(0)
     small = ["s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
              "rescan_s2"]
-    tiled = ["t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3a_lists_targets", "t_s3b_window",
+    tiled = ["t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3_lists_targets_window", "t_s3_overflow",
              "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2"]
     rows = []
 
