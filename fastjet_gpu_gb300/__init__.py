@@ -234,7 +234,8 @@ class Context:
               "rescan_s2", "steps", "events", "exact_argmin", "exact_closer",
               "t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3_lists_targets_window", "t_s3_overflow",
               "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2", "t_steps", "t_events", "exact_key", "exact_nn",
-              "t_targets", "t_target_steps")
+              "t_targets", "t_target_steps", "t_list_update", "t_targets_warp1", "t_window_thread0",
+              "t_resolve_new_jet", "t_summary_new_jet_tile", "t_summaries_warp1")
 
     def phase_clocks(self, reset=False):
         """Per-step phase counters of the clustering kernels (only in the

@@ -64,6 +64,10 @@ enum PhaseSlot {
   kPhTRebuild = 12, kPhTS1, kPhTS2, kPhTS3a, kPhTS3b, kPhTS3c, kPhTKin, kPhTDetect, kPhTSteps, kPhTEvents,
   // the tiled kernel's targets: summed over steps, and steps that had any
   kPhTTargets = 24, kPhTTargetSteps,
+  // inside the tiled kernel's S3 and S3c: thread 0's list update, warp 1's
+  // targets, thread 0's share of the window pass; warp 0's resolution of the
+  // new jet's neighbour and its tile's summary, warp 1's other summaries
+  kPhTListUpd = 26, kPhTTargetsW1, kPhTWindowT0, kPhTResolveA, kPhTSumA, kPhTSumW1,
   kPhSlots = 32
 };
 #ifdef FJG_PHASE_CLOCKS

@@ -71,8 +71,12 @@
 //       then compare every slot of the new jet's window with it (targets,
 //       flagged in S2, are left to their own searches).                   B3
 //       (targets beyond the listed ones: a second pass, then a barrier)
-//   S3c warp 0 resolves the new jet's neighbour and then re-summarises its
-//       tile; the other warps re-summarise the other changed tiles.       B4
+//   S3c warp 0 resolves the new jet's neighbour while warp 1 summarises the
+//       new jet's tile without it; warp 0 then merges the new jet's key in
+//       (merge_skipped).  The other warps re-summarise the other changed
+//       tiles (a winner there whose neighbour is the new jet may read the
+//       new jet's fields mid-update: they only decide whether the new jet is
+//       left out of that tile's second bound, and it is no member there). B4
 #pragma once
 
 #include "fjg_cluster.cuh"
@@ -110,6 +114,15 @@ struct alignas(16) TileSum {
   float m2;
   int nnk;
   int pad0, pad1, pad2;
+};
+
+// Summary parts of a tile's members other than one slot (tile_part).
+struct TilePart {
+  float m1;
+  int x;
+  float u1;
+  int nnk;
+  float mo;
 };
 
 constexpr int kNoNeighbour = 0x7fffffff;    // neighbour field without a neighbour
@@ -237,6 +250,7 @@ struct TiledShared {
   int event, ctl_njets;
   double red[3][W];
   int scan_tmp[W];
+  TilePart part;  // the new jet's tile without the new jet (S3c)
   // the event's tile lists' ranges and the tile summaries (LargeWs points here)
   int t_start[kSmemTiles], t_count[kSmemTiles];
   TileSum tsum[kSmemTiles];
@@ -454,11 +468,17 @@ __device__ __forceinline__ int resolve_large(const TiledShared& S, const LargeWs
   return r.idx;
 }
 
-// Summary of tile tt (whole warp).  Each lane keeps its two smallest lower
-// bounds with their slots and the third smallest bound, reading four members
-// per pass; the winner's neighbour field (and its neighbour's, to recognise
-// a mutual partner) is read once at the end.
-__device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
+// Summary parts of the members of tile tt other than `skip` (whole warp;
+// every lane receives them): the smallest key lower bound m1 and its slot x
+// (the lowest among equal bounds) with x's key upper bound and neighbour
+// field, and mo, the smallest lower bound of the other members without x's
+// mutual partner.  Each lane keeps its two smallest bounds with their slots
+// and the third smallest bound, reading four members per pass; x's neighbour
+// field (and its neighbour's, to recognise a mutual partner) is read once at
+// the end.  When x's neighbour is `skip` (a slot whose state another warp may
+// be writing) its fields are not read: mo then leaves out x alone, and
+// merge_skipped decides the partner once skip's state is known.
+__device__ __forceinline__ TilePart tile_part(const LargeWs& L, int tt, int skip) {
   constexpr int B = 4;
   const int lane = threadIdx.x & 31;
   const float inf = __int_as_float(0x7f800000);
@@ -469,7 +489,10 @@ __device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
     int u[B];
     float lo[B];
 #pragma unroll
-    for (int q = 0; q < B; ++q) u[q] = i0 + 32 * q < m ? L.members[base + i0 + 32 * q] : -1;
+    for (int q = 0; q < B; ++q) {
+      u[q] = i0 + 32 * q < m ? L.members[base + i0 + 32 * q] : -1;
+      if (u[q] == skip) u[q] = -1;
+    }
 #pragma unroll
     for (int q = 0; q < B; ++q) lo[q] = u[q] >= 0 ? L.klo[u[q]] : inf;
 #pragma unroll
@@ -501,13 +524,40 @@ __device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
     const bool px = L.pair[x] != 0;
     u1 = L.khi[x];
     nnk = (nx < 0 ? kNoNeighbour : nx) | (px ? (int)kPairBit : 0);
-    if (px && nx >= 0 && L.pair[nx] != 0 && L.nn[nx] == x) p = nx;
+    if (px && nx >= 0 && nx != skip && L.pair[nx] != 0 && L.nn[nx] == x) p = nx;
   }
   p = __shfl_sync(kFull, p, 0);
   // smallest bound of the lane's members other than the winner and its partner
   const float contrib = (s1 >= 0 && s1 != x && s1 != p) ? m1 : (s2 >= 0 && s2 != x && s2 != p) ? m2 : m3;
   const float mo = __uint_as_float(__reduce_min_sync(kFull, __float_as_uint(contrib)));
-  if (lane == 0) L.tsum[tt] = TileSum{__uint_as_float(mb), x, u1, mo, nnk, 0, 0, 0};
+  return TilePart{__uint_as_float(mb), x, __shfl_sync(kFull, u1, 0), __shfl_sync(kFull, nnk, 0), mo};
+}
+
+// Summary of tile tt (whole warp).
+__device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
+  const TilePart P = tile_part(L, tt, -1);
+  if ((threadIdx.x & 31) == 0) L.tsum[tt] = TileSum{P.m1, P.x, P.u1, P.mo, P.nnk, 0, 0, 0};
+}
+
+// The summary of a tile from the parts of its members other than slot a
+// (tile_part with skip = a) and a's own key and neighbour field.  a wins by
+// (klo, slot); the second bound leaves out the winner's mutual partner, and
+// two slots are mutual partners exactly when each one's neighbour field names
+// the other with the pair bit -- so no further state is read.
+//   a wins: the smallest other bound is P's winner's, unless that winner is
+//     a's mutual partner; then its field names a, P.mo left out P.x alone,
+//     and P.mo is the bound.
+//   P.x wins: P.mo left out P.x and its partner, a included when P.x's field
+//     does not name a (then a is neither); when it names a, P.mo left out P.x
+//     alone, and a's bound counts unless a is the mutual partner.
+__device__ __forceinline__ TileSum merge_skipped(const TilePart& P, int a, float ka, float ua, int nnka) {
+  const int a_pair = (int)((unsigned)a | kPairBit);
+  if (P.x < 0 || ka < P.m1 || (ka == P.m1 && (unsigned)a < (unsigned)P.x)) {
+    const bool mutual = P.x >= 0 && P.nnk == a_pair && nnka == (int)((unsigned)P.x | kPairBit);
+    return TileSum{ka, a, ua, mutual ? P.mo : P.m1, nnka, 0, 0, 0};
+  }
+  const bool mutual = P.nnk == a_pair && nnka == (int)((unsigned)P.x | kPairBit);
+  return TileSum{P.m1, P.x, P.u1, mutual ? P.mo : fminf(P.mo, ka), P.nnk, 0, 0, 0};
 }
 
 // Block-wide rebuild of the tile lists from the live slots (S.slack free
@@ -750,7 +800,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
   int n = N;
   int step = 0;
   FJG_PH(long long ph_rb = 0, ph_s1 = 0, ph_s2 = 0, ph_s3a = 0, ph_s3b = 0, ph_s3c = 0, ph_kin = 0, ph_det = 0;
-         long long ph_tg = 0, ph_tgs = 0;)
+         long long ph_tg = 0, ph_tgs = 0, ph_lu = 0, ph_tt = 0, ph_wp = 0, ph_ra = 0, ph_sa = 0, ph_so = 0;)
   while (n > 0) {
     FJG_PH(const long long ph0 = clock64();)
     if (step > 0 && step % S.slack == 0) rebuild_tiles(S, L, N);
@@ -939,6 +989,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     // S3a: tile lists (thread 0: a tombstone for b, and for a when it
     // changes tile, then an append); targets (one warp each)
     if (tid == 0) {
+      FJG_PH(const long long q0 = clock64();)
       // every word the update reads is loaded before its first store: the
       // arrays are distinct, but the compiler cannot know that the stores to
       // the member lists leave them alone, and would otherwise wait for each
@@ -964,8 +1015,10 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           mark_dirty(S, ta);
         }
       }
+      FJG_PH(ph_lu += clock64() - q0;)
     }
     // targets go to warps 1, 2, ... first: warp 0's thread 0 is busy above
+    FJG_PH(const long long q1 = clock64();)
     for (int r = (warp + W - 1) % W; r < nr_all; r += W) {
       const int t = S.rlist[r];
       Cert x = cert_empty();
@@ -992,6 +1045,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       }
       __syncwarp();
     }
+    FJG_PH(const long long q2 = clock64(); if (warp == 1 && lane == 0) ph_tt += q2 - q1;)
     // S3b, in the same phase: every slot of the new jet's window against the
     // new jet, beside the list update and the targets' searches (no barrier
     // between them).  This step's targets (alive == 2, set before B2) are
@@ -1059,6 +1113,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       const Cert wc = cert_warp(ca);
       if (lane == 0) S.wcert[warp] = wc;
     }
+    FJG_PH(if (tid == 0) ph_wp += clock64() - q2;)
     __syncthreads();  // B3: lists updated, listed targets done, the new jet's window compared
     FJG_PH(const long long ph3 = clock64(); ph_s3a += ph3 - ph2;)
     if (n_found > kMaxListed) {
@@ -1094,23 +1149,36 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     // S3c: the new jet's neighbour (warp 0, then its tile's summary) and the
     // other changed tiles' summaries (the remaining warps)
     const int nd = S.n_dirty;
+    FJG_PH(const long long q5 = clock64();)
+    if (pair && warp == 1) {
+      // the new jet's tile without the new jet, while warp 0 resolves it
+      // (tile_part reads none of the new jet's state)
+      const TilePart P = tile_part(L, ta, a);
+      if (lane == 0) S.part = P;
+      named_sync(3, 64);
+    }
     if (pair && warp == 0) {
+      FJG_PH(const long long q3 = clock64();)
       Cert x = (lane < W) ? S.wcert[lane] : cert_empty();
       x = cert_warp(x);
       float lo, hi;
       const int nn = resolve_large(S, L, X, a, x, b, -1, -1, lo, hi);
+      int nnka = kNoNeighbour;
       if (lane == 0) {
         if (nn >= 0) atomicAdd(&L.rc[nn], 1);
         L.nn[a] = nn;
         L.nlo[a] = lo;
         L.nhi[a] = hi;
         set_key_large(L, X, a);
+        nnka = (nn < 0 ? kNoNeighbour : nn) | (L.pair[a] != 0 ? (int)kPairBit : 0);
       }
-      __syncwarp();
-      tile_summary(L, ta);
+      FJG_PH(const long long q4 = clock64(); if (lane == 0) ph_ra += q4 - q3;)
+      named_sync(3, 64);  // warp 1's parts are in S.part
+      if (lane == 0) L.tsum[ta] = merge_skipped(S.part, a, L.klo[a], L.khi[a], nnka);
+      FJG_PH(if (lane == 0) ph_sa += clock64() - q4;)
     }
-    if (!(pair && warp == 0)) {
-      const int w0 = pair ? 1 : 0;  // warps taking part: w0 .. W-1
+    if (!pair || warp >= 2) {
+      const int w0 = pair ? 2 : 0;  // warps taking part: w0 .. W-1
       if (nd > kMaxDirty) {
         for (int t = warp - w0; t < S.nt; t += W - w0)
           if (t != ta) tile_summary(L, t);
@@ -1119,6 +1187,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
           if (S.dirty[k] != ta) tile_summary(L, S.dirty[k]);
       }
     }
+    FJG_PH(if (warp == 1 && lane == 0) ph_so += clock64() - q5;)
     __syncthreads();  // B4
     FJG_PH(ph_s3c += clock64() - ph4;)
     if (nd > kMaxDirty) {
@@ -1152,6 +1221,16 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     }
     if (warp == 1 && lane == 0) atomicAdd(A.phase + kPhTKin, (unsigned long long)ph_kin);
     if (tid == 32 * MW) atomicAdd(A.phase + kPhTDetect, (unsigned long long)ph_det);
+    if (tid == 0) {
+      atomicAdd(A.phase + kPhTListUpd, (unsigned long long)ph_lu);
+      atomicAdd(A.phase + kPhTWindowT0, (unsigned long long)ph_wp);
+      atomicAdd(A.phase + kPhTResolveA, (unsigned long long)ph_ra);
+      atomicAdd(A.phase + kPhTSumA, (unsigned long long)ph_sa);
+    }
+    if (warp == 1 && lane == 0) {
+      atomicAdd(A.phase + kPhTTargetsW1, (unsigned long long)ph_tt);
+      atomicAdd(A.phase + kPhTSumW1, (unsigned long long)ph_so);
+    }
   })
   if (A.owner) {
     for (int s = tid; s < N; s += T) {

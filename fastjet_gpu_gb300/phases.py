@@ -28,7 +28,12 @@ tile summaries), t_s2_merge_detect (merge || target detection and scans),
 t_s3_lists_targets_window (list update, targets, the new jet against its
 window), t_s3_overflow (targets beyond the listed ones, flags), t_s3c_summaries (changed tiles, the new jet's neighbour); inside t_s2:
 t_kin_rapidity (the rapidity chain) and t_detect_s2 (the first detection
-thread's work).
+thread's work); inside t_s3: t_list_update (thread 0), t_targets_warp1 (warp
+1's targets), t_window_thread0 (thread 0's share of the window pass); inside
+t_s3c_summaries: t_resolve_new_jet and t_summary_new_jet_tile (warp 0: its
+wait for warp 1 and the merge of the new jet's key), t_summaries_warp1 (warp 1:
+the new jet's tile without the new jet, or on promotion steps its share of the
+changed tiles).
 """
 from __future__ import annotations
 
@@ -57,7 +62,8 @@ def main():
     small = ["s1_argmin", "s2_merge", "s3_new_jet", "tail_resolve", "kin_warp0", "kin_warp1", "kin_warp2",
              "rescan_s2"]
     tiled = ["t_rebuild", "t_s1_argmin", "t_s2_merge_detect", "t_s3_lists_targets_window", "t_s3_overflow",
-             "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2"]
+             "t_s3c_summaries", "t_kin_rapidity", "t_detect_s2", "t_list_update", "t_targets_warp1",
+             "t_window_thread0", "t_resolve_new_jet", "t_summary_new_jet_tile", "t_summaries_warp1"]
     rows = []
 
     def report(tag, c):
