@@ -179,10 +179,21 @@ __device__ __forceinline__ Cand cand_warp(const Cand& c) {
   return r;
 }
 
+// One float of a slot's geometry record (a strided view: float i of record
+// s is p[4 s]), so that single fields read and write as from an array.
+struct RecField {
+  float* p;
+  __device__ __forceinline__ float& operator[](int s) const { return p[4 * (int64_t)s]; }
+};
+
 // Per-event large workspace: pointers into the event's region of
-// large_ws_bytes(N) bytes.
+// large_ws_bytes(N) bytes.  The window scans read a member's coordinates and
+// neighbour interval together, so those four floats sit in one 16 B record
+// per slot (one sector per lane for a warp's gather, not four).
 struct LargeWs {
-  float *rap32, *phi32, *wlo, *whi, *nlo, *nhi, *klo, *khi;  // [N]
+  float4* geo;                           // [N] rap32, phi32, nlo, nhi
+  RecField rap32, phi32, nlo, nhi;       // views of geo's fields
+  float *wlo, *whi, *klo, *khi;                               // [N]
   int *nn, *tile, *pos;                                       // [N]
   int* rc;                                                    // [N] slots whose neighbour this is
   int8_t *pair, *alive;                                       // [N]
@@ -205,12 +216,13 @@ __device__ __forceinline__ LargeWs large_ws(unsigned char* base, int N) {
   LargeWs L;
   const int MT = large_max_tiles(N);
   float* f = reinterpret_cast<float*>(base);
-  L.rap32 = f;
-  L.phi32 = f + N;
-  L.wlo = f + 2 * N;
-  L.whi = f + 3 * N;
-  L.nlo = f + 4 * N;
-  L.nhi = f + 5 * N;
+  L.geo = reinterpret_cast<float4*>(f);  // 16 B aligned: the region starts at a multiple of 96 B
+  L.rap32 = RecField{f};
+  L.phi32 = RecField{f + 1};
+  L.nlo = RecField{f + 2};
+  L.nhi = RecField{f + 3};
+  L.wlo = f + 4 * N;
+  L.whi = f + 5 * N;
   L.klo = f + 6 * N;
   L.khi = f + 7 * N;
   int* i = reinterpret_cast<int*>(f + 8 * N);
@@ -407,8 +419,9 @@ __device__ __forceinline__ void window_cert(const TiledShared& S, const LargeWs&
 #pragma unroll
     for (int k = 0; k < kMaxWindowTiles; ++k) {
       if (u[k] >= 0) {
-        r[k] = L.rap32[u[k]];
-        ph[k] = L.phi32[u[k]];
+        const float2 g2 = *reinterpret_cast<const float2*>(L.geo + u[k]);
+        r[k] = g2.x;
+        ph[k] = g2.y;
       }
     }
 #pragma unroll
@@ -1069,11 +1082,12 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
 #pragma unroll
         for (int k = 0; k < NT; ++k) {
           if (u[k] >= 0) {
-            r[k] = L.rap32[u[k]];
-            ph[k] = L.phi32[u[k]];
+            const float4 g4 = L.geo[u[k]];
+            r[k] = g4.x;
+            ph[k] = g4.y;
+            nl[k] = g4.z;
+            nh[k] = g4.w;
             cn[k] = L.nn[u[k]];
-            nl[k] = L.nlo[u[k]];
-            nh[k] = L.nhi[u[k]];
             al[k] = L.alive[u[k]];
           }
         }

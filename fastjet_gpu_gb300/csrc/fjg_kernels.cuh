@@ -122,7 +122,7 @@ struct Scratch {
   double* ws;         // [kWsFields][ws_stride] exact per-particle state
   int64_t ws_stride;  // particles the workspace holds
   int32_t* hist;      // [kHistBins] events per size, then per-size positions (sorting by size)
-  unsigned char* large_ws;    // kLargeWsBytesPerParticle per particle (null: large events are refused)
+  unsigned char* large_ws;    // kLargeWsBytesPerParticle per particle, 16 B aligned (null: large events are refused)
   int64_t large_ws_particles;  // particles the large workspace covers
 };
 

@@ -26,6 +26,7 @@
 // large_ws_bytes(N) <= 91 N + 31 < kLargeWsBytesPerParticle * N bytes from
 // kLargeWsBytesPerParticle * offsets[e] on, so its region ends inside the
 // large workspace too (no margin is needed past the last particle).
+#include <cstddef>
 #include <cstdint>
 #include <mutex>
 
@@ -51,6 +52,7 @@ struct NoAllocScratch {
 };
 
 static_assert(sizeof(NoAllocScratch) <= FJG_NOALLOC_SCRATCH_BYTES, "scratch larger than documented");
+static_assert(offsetof(NoAllocScratch, large_ws) % 16 == 0, "the tiled kernel reads 16 B records from large_ws");
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
