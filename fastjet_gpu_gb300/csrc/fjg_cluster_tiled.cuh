@@ -185,18 +185,30 @@ struct RecField {
   float* p;
   __device__ __forceinline__ float& operator[](int s) const { return p[4 * (int64_t)s]; }
 };
+struct RecInt {
+  int* p;
+  __device__ __forceinline__ int& operator[](int s) const { return p[4 * (int64_t)s]; }
+};
+struct RecByte {
+  int8_t* p;
+  __device__ __forceinline__ int8_t& operator[](int s) const { return p[16 * (int64_t)s]; }
+};
 
 // Per-event large workspace: pointers into the event's region of
 // large_ws_bytes(N) bytes.  The window scans read a member's coordinates and
 // neighbour interval together, so those four floats sit in one 16 B record
-// per slot (one sector per lane for a warp's gather, not four).
+// per slot (one sector per lane for a warp's gather, not four); its
+// neighbour, key interval, kind and liveness in a second one.
 struct LargeWs {
   float4* geo;                           // [N] rap32, phi32, nlo, nhi
   RecField rap32, phi32, nlo, nhi;       // views of geo's fields
-  float *wlo, *whi, *klo, *khi;                               // [N]
-  int *nn, *tile, *pos;                                       // [N]
+  int4* meta;                            // [N] nn, klo, khi (float bits), flags (byte 0 pair, byte 1 alive)
+  RecInt nn;                             // views of meta's fields
+  RecField klo, khi;
+  RecByte pair, alive;
+  float *wlo, *whi;                                           // [N]
+  int *tile, *pos;                                            // [N]
   int* rc;                                                    // [N] slots whose neighbour this is
-  int8_t *pair, *alive;                                       // [N]
   int* members;                                               // [N + kListSlack * MT]
   int *t_start, *t_count;                                     // [MT] (the kernel points these
   TileSum* tsum;                                              // [MT]  three at shared memory)
@@ -208,7 +220,7 @@ __host__ __device__ __forceinline__ int large_max_tiles(int N) { return (N / 8 <
 
 __host__ __device__ __forceinline__ int64_t large_ws_bytes(int N) {
   const int64_t MT = large_max_tiles(N);
-  const int64_t head = 8 * 4 * (int64_t)N + 4 * 4 * (int64_t)N + ((2 * (int64_t)N + 15) & ~(int64_t)15);
+  const int64_t head = 52 * (int64_t)N;  // two 16 B records, two floats and three ints per slot
   return head + 4 * ((int64_t)N + kListSlack * MT) + 2 * 4 * MT + 16 + 32 * MT;
 }
 
@@ -221,19 +233,20 @@ __device__ __forceinline__ LargeWs large_ws(unsigned char* base, int N) {
   L.phi32 = RecField{f + 1};
   L.nlo = RecField{f + 2};
   L.nhi = RecField{f + 3};
-  L.wlo = f + 4 * N;
-  L.whi = f + 5 * N;
-  L.klo = f + 6 * N;
-  L.khi = f + 7 * N;
-  int* i = reinterpret_cast<int*>(f + 8 * N);
-  L.nn = i;
-  L.tile = i + N;
-  L.pos = i + 2 * N;
-  L.rc = i + 3 * N;
-  int8_t* b = reinterpret_cast<int8_t*>(i + 4 * N);
-  L.pair = b;
-  L.alive = b + N;
-  int* m = reinterpret_cast<int*>(b + ((2 * N + 15) & ~15));
+  L.meta = reinterpret_cast<int4*>(f + 4 * N);
+  int* mi = reinterpret_cast<int*>(L.meta);
+  L.nn = RecInt{mi};
+  L.klo = RecField{f + 4 * N + 1};
+  L.khi = RecField{f + 4 * N + 2};
+  L.pair = RecByte{reinterpret_cast<int8_t*>(mi + 3)};
+  L.alive = RecByte{reinterpret_cast<int8_t*>(mi + 3) + 1};
+  L.wlo = f + 8 * N;
+  L.whi = f + 9 * N;
+  int* i = reinterpret_cast<int*>(f + 10 * N);
+  L.tile = i;
+  L.pos = i + N;
+  L.rc = i + 2 * N;
+  int* m = i + 3 * N;
   L.members = m;
   L.t_start = m + N + kListSlack * MT;
   L.t_count = L.t_start + MT;
@@ -533,11 +546,15 @@ __device__ __forceinline__ TilePart tile_part(const LargeWs& L, int tt, int skip
   int nnk = kNoNeighbour, p = -1;
   float u1 = inf;
   if (lane == 0 && x >= 0) {
-    const int nx = L.nn[x];
-    const bool px = L.pair[x] != 0;
-    u1 = L.khi[x];
+    const int4 mx = L.meta[x];
+    const int nx = mx.x;
+    const bool px = (int8_t)mx.w != 0;
+    u1 = __int_as_float(mx.z);
     nnk = (nx < 0 ? kNoNeighbour : nx) | (px ? (int)kPairBit : 0);
-    if (px && nx >= 0 && nx != skip && L.pair[nx] != 0 && L.nn[nx] == x) p = nx;
+    if (px && nx >= 0 && nx != skip) {
+      const int4 mn = L.meta[nx];
+      if ((int8_t)mn.w != 0 && mn.x == x) p = nx;
+    }
   }
   p = __shfl_sync(kFull, p, 0);
   // smallest bound of the lane's members other than the winner and its partner
@@ -1087,8 +1104,9 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
             ph[k] = g4.y;
             nl[k] = g4.z;
             nh[k] = g4.w;
-            cn[k] = L.nn[u[k]];
-            al[k] = L.alive[u[k]];
+            const int4 m4 = L.meta[u[k]];
+            cn[k] = m4.x;
+            al[k] = (int8_t)(m4.w >> 8);
           }
         }
 #pragma unroll

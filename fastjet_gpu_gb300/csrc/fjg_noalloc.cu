@@ -23,7 +23,7 @@
 // Bounds: the input check refuses events whose range [offsets[e],
 // offsets[e+1]) leaves [0, total) (total <= kNoAllocMaxParticles, the extent
 // of the per-particle workspace) and reads no momentum past `total`.  An event above 4096 particles uses
-// large_ws_bytes(N) <= 91 N + 31 < kLargeWsBytesPerParticle * N bytes from
+// large_ws_bytes(N) <= 93 N + 16 < kLargeWsBytesPerParticle * N bytes from
 // kLargeWsBytesPerParticle * offsets[e] on, so its region ends inside the
 // large workspace too (no margin is needed past the last particle).
 #include <cstddef>
