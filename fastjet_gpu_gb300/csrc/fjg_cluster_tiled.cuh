@@ -269,6 +269,7 @@ struct TiledShared {
   Cert rcert[kTiledTargets][W];
   int rlist[kMaxListed];
   int n_rescan;
+  int win_next;  // the window pass's next chunk of list positions (S3)
   int dirty[kMaxDirty];
   int n_dirty;
   unsigned dirty_bits[kMaxTiles / 32];
@@ -767,6 +768,7 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     S.ctl_njets = 0;
     S.n_rescan = 0;
     S.n_dirty = 0;
+    S.win_next = 0;
   }
   {
     double rmax = 0.0;
@@ -1091,7 +1093,15 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
       const float ra = L.rap32[a], pa = L.phi32[a];
       constexpr int NT = kMaxWindowTiles;
       const TileRanges<NT> R = tile_ranges<NT>(L, tiles, nw);
-      for (int i = tid; i < R.maxlen; i += T) {
+      // list positions go out 32 at a time from a shared counter, so that
+      // the warps that ran the list update or a target come late and take
+      // fewer (each warp takes chunks until the longest list is covered)
+      for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&S.win_next, 32);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= R.maxlen) break;
+        const int i = base + lane;
         int u[NT], cn[NT], al[NT];
         float r[NT], ph[NT], nl[NT], nh[NT];
 #pragma unroll
@@ -1230,8 +1240,9 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
     if (tid == 0) {
       S.n_rescan = 0;
       S.n_dirty = 0;
+      S.win_next = 0;
     }
-    // the next reads of dirty_bits, n_rescan and n_dirty follow B1 and B2
+    // the next reads of dirty_bits, n_rescan, n_dirty and win_next follow B1 and B2
   }
 
   // ---- epilogue: jet count, and constituent ownership from the union-find
