@@ -172,3 +172,21 @@ def test_workload_size_events_match_oracle(ctx):
             o = b.offsets[e]
             assert np.array_equal(res["jets"][o:o + nj[e]], jets[o:o + nj[e]]), (algo, e)
             assert np.array_equal(res["jet_label"][o:o + nj[e]], lab[o:o + nj[e]]), (algo, e)
+
+
+def test_tile_count_cap_event_matches_oracle(ctx):
+    """A 40k-particle pile-up-like event at anti-kt R=0.1 would want ~1,240
+    tiles of side 0.2 (32 particles a tile); the tiled kernel keeps at most
+    1024 (its tile ranges and summaries live in shared memory) and halves the
+    rapidity rows instead.  Merge history, jets and constituents identical bit
+    for bit to the oracle (portable kinematics)."""
+    import oracle
+    b = E._batch_from([E.portable_event(40000, 4, seed=77)])
+    res = ctx.cluster_batch(b.particles, b.offsets, -1, 0.1, history=True, owner=True)
+    hist, jets, lab, own, nj, _ = oracle.cluster_batch(b.particles, b.offsets, -1, 0.1, threads=1, portable=True)
+    assert np.array_equal(res["n_jets"], nj)
+    assert np.array_equal(res["history"]["a"], hist["a"]) and np.array_equal(res["history"]["b"], hist["b"])
+    assert np.array_equal(res["history"]["d"], hist["d"])
+    assert np.array_equal(res["owner"], own)
+    assert np.array_equal(res["jets"][:nj[0]], jets[:nj[0]])
+    assert np.array_equal(res["jet_label"][:nj[0]], lab[:nj[0]])
