@@ -981,6 +981,9 @@ __device__ inline void cluster_event_tiled(TiledShared& S, const BatchArgs& A, u
         constexpr int NU = 2 * kMaxWindowTiles;
         const TileRanges<NU> R = tile_ranges<NU>(L, tiles, nw);
         for (int i = r0; i < R.maxlen; i += TR) {
+          // the referrer counts say how many targets there are: once all are
+          // found, the remaining passes would find none
+          if (*(volatile int*)&S.n_rescan >= expected) break;
           int u[NU], nu[NU];
   #pragma unroll
           for (int k = 0; k < NU; ++k) u[k] = i < R.len[k] ? L.members[R.start[k] + i] : -1;
