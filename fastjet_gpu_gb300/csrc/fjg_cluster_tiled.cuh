@@ -1,6 +1,8 @@
 // Clustering of large events (more than 4096 particles): one CTA per event,
-// state in a global workspace, nearest neighbours restricted to a 3x3 window
-// of rapidity-azimuth tiles.  (The reference's grid backend, grid.cu:55-549,
+// per-slot state in a global workspace (two 16 B records per slot, read with
+// one gather each), the tile lists' ranges and the tile summaries in shared
+// memory, nearest neighbours restricted to a 3x3 window of rapidity-azimuth
+// tiles.  (The reference's grid backend, grid.cu:55-549,
 // also tiles the plane with cells of side >= R and compares adjacent cells;
 // it keeps per-cell pair minima, this kernel a per-slot neighbour table.)
 //
@@ -68,8 +70,9 @@
 //       of c's and j's tiles) and scan the first 32 of them.               B2
 //   S3  thread 0 updates the tile lists; the warps finish the targets'
 //       neighbours, adding the new jet when it lies in their window, and
-//       then compare every slot of the new jet's window with it (targets,
-//       flagged in S2, are left to their own searches).                   B3
+//       then compare every slot of the new jet's window with it, taking the
+//       window's list positions in chunks of 32 (targets, flagged in S2, are
+//       left to their own searches).                                      B3
 //       (targets beyond the listed ones: a second pass, then a barrier)
 //   S3c warp 0 resolves the new jet's neighbour while warp 1 summarises the
 //       new jet's tile without it; warp 0 then merges the new jet's key in
