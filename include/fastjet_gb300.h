@@ -105,11 +105,15 @@ const char* fjg_last_error(const fjg_ctx* ctx);
  * out[23] how many FP64 fallbacks the argmin, the closer-neighbour tests, the
  * key updates and the neighbour searches took.  Tiled kernel (events above
  * 4096 particles): out[12..17] cycles in the list rebuilds, the argmin, the
- * merge and target detection, the list update and targets, the new jet's
- * window pass, the tile summaries; out[18] in the rapidity chain, out[19] in
- * the first detection thread's merge-phase work, out[20] steps, out[21]
- * events, out[24] targets found (slots whose neighbour was merged) and
- * out[25] steps with any (n <= 32 entries).  Only a library built with
+ * merge and target detection, the list update with the targets and the new
+ * jet's window pass, the pass for targets beyond the listed ones, the tile
+ * summaries; out[18] in the rapidity chain, out[19] in the first detection
+ * thread's merge-phase work, out[20] steps, out[21] events, out[24] targets
+ * found (slots whose neighbour was merged) and out[25] steps with any;
+ * out[26..28] thread 0's list update, warp 1's targets and thread 0's share
+ * of the window pass; out[29..31] warp 0's resolution of the new jet's
+ * neighbour and its merge into its tile's summary, and warp 1's summary work
+ * (n <= 32 entries).  Only a library built with
  * -DFJG_PHASE_CLOCKS (python -m fastjet_gpu_gb300.build --phase-clocks) has
  * them; the product build returns FJG_EINVAL.  Waits for the context stream;
  * `reset` zeroes them.  No counterpart in the reference. */
