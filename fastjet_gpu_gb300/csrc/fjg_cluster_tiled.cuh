@@ -584,7 +584,7 @@ __device__ __forceinline__ void tile_summary(const LargeWs& L, int tt) {
 //   P.x wins: P.mo left out P.x and its partner, a included when P.x's field
 //     does not name a (then a is neither); when it names a, P.mo left out P.x
 //     alone, and a's bound counts unless a is the mutual partner.
-__device__ __forceinline__ TileSum merge_skipped(const TilePart& P, int a, float ka, float ua, int nnka) {
+__host__ __device__ __forceinline__ TileSum merge_skipped(const TilePart& P, int a, float ka, float ua, int nnka) {
   const int a_pair = (int)((unsigned)a | kPairBit);
   if (P.x < 0 || ka < P.m1 || (ka == P.m1 && (unsigned)a < (unsigned)P.x)) {
     const bool mutual = P.x >= 0 && P.nnk == a_pair && nnka == (int)((unsigned)P.x | kPairBit);
